@@ -1,0 +1,202 @@
+/*
+ * mkg_tissue.h -- C ABI of the GB300 tissue-simulation host library.
+ *
+ * This library replaces the per-simulation CPython module that myokit
+ * generates from myokit/_sim/openclsim.c (module methods sim_init, sim_step
+ * and sim_clean, openclsim.c:1216-1221) and the OpenCL runtime calls made
+ * inside it. The arguments of sim_init (openclsim.c:385-407) are split over
+ * one call per input so that every buffer crosses the boundary once, as a
+ * plain pointer plus a size, instead of as a Python list of floats.
+ *
+ * Conventions
+ *  - Every function returns an int status: MKG_OK (0), a positive run status
+ *    (mkg_run_chunk only) or a negative error code. No function aborts.
+ *  - After an error, mkg_last_error() returns a message for the handle (or
+ *    for the thread, when no handle was created).
+ *  - Host arrays are read or written only during the call; the library keeps
+ *    no pointer to caller memory.
+ *  - State vectors are "array of structures" doubles with the x index
+ *    running fastest, the layout used by SimulationOpenCL.state()
+ *    (openclsim.py:1727-1757). The device stores them as structure of arrays.
+ *  - One handle owns one CUDA stream and its device buffers. A handle is not
+ *    thread safe; different handles may be used from different threads.
+ */
+#ifndef MKG_TISSUE_H
+#define MKG_TISSUE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes */
+#define MKG_OK              0
+#define MKG_DONE            1   /* run reached tmax (sim_step's final return) */
+#define MKG_HALT_NAN        2   /* NaN halt: openclsim.c:1086-1089, 1199-1204 */
+#define MKG_ERR_ARG        -1   /* invalid argument or size */
+#define MKG_ERR_CUDA       -2   /* CUDA runtime error */
+#define MKG_ERR_COMPILE    -3   /* NVRTC compilation failed (log in mkg_last_error) */
+#define MKG_ERR_PACING     -4   /* invalid protocol (pacing.h ESys_POPULATE_*) */
+#define MKG_ERR_TIMEOUT    -5   /* a bounded device-side wait ran out */
+#define MKG_ERR_ORDER      -6   /* call made in the wrong order */
+#define MKG_ERR_SIMULTANEOUS -7 /* two events at the same time (pacing.h:204-206) */
+#define MKG_ERR_NOMEM      -8   /* host or device allocation failed */
+
+/* Diffusion modes, one per reference kernel (openclsim.cl:384-573) */
+#define MKG_DIFF_NONE       0   /* diffusion=False */
+#define MKG_DIFF_GRID       1   /* diff_step: homogeneous 1D/2D grid */
+#define MKG_DIFF_HETERO     2   /* diff_hetero: per-edge conductances */
+#define MKG_DIFF_CONN       3   /* diff_arb_step: arbitrary connections */
+
+/* Pacing modes (calculate_pacing, openclsim.cl:249-280, 325-330) */
+#define MKG_PACE_ALL        0   /* diffusion disabled: every cell gets pace */
+#define MKG_PACE_RECT       1   /* rectangle from set_paced_cells */
+#define MKG_PACE_LIST       2   /* explicit cell list from set_paced_cell_list */
+#define MKG_PACE_NONE       3   /* diffusion enabled, empty list: pace 0 */
+
+/* Log items: what one log column records (openclsim.c:916-1022) */
+#define MKG_ITEM_IDIFF(n_state)       (n_state)
+#define MKG_ITEM_INTER(n_state, k)    ((n_state) + 1 + (k))
+
+typedef struct mkg_sim mkg_sim;
+
+/* Configuration fixed when the simulation program is built. */
+typedef struct mkg_config {
+    int64_t nx;             /* cells in x (sim_init nx, openclsim.c:389) */
+    int64_t ny;             /* cells in y; 1 for 1D (openclsim.c:390) */
+    int32_t real_bytes;     /* 4 = single, 8 = double precision */
+    int32_t n_state;        /* states per cell (openclsim.cl "n_state") */
+    int32_t n_inter;        /* logged intermediaries the kernel writes */
+    int32_t n_field;        /* scalar fields (openclsim.cl "n_field") */
+    int32_t i_vm;           /* index of V in the state; -1 without diffusion */
+    int32_t diffusion;      /* MKG_DIFF_* */
+    int32_t block_x;        /* CTA shape the kernel was generated for */
+    int32_t block_y;
+    int32_t device;         /* CUDA device ordinal */
+    int32_t two_d;          /* 1: kernel tiles an (nx, ny) grid with
+                               (block_x, block_y) CTAs; 0: cells are a
+                               flat array covered by (block_x, 1) CTAs */
+} mkg_config;
+
+/*
+ * Compiles generated CUDA C++ source to an sm_103a cubin with NVRTC.
+ * Replaces clCreateProgramWithSource + clBuildProgram (openclsim.c:812-839).
+ * On success *cubin (size *cubin_size) and *log are malloc'd; free them with
+ * mkg_free. On a compile failure the return is MKG_ERR_COMPILE and *log
+ * holds the compiler output.
+ */
+int mkg_compile(const char *source, const char *name,
+                const char *const *options, int n_options,
+                void **cubin, size_t *cubin_size, char **log);
+void mkg_free(void *ptr);
+
+/*
+ * Creates a simulation from a cubin produced by mkg_compile. Allocates the
+ * device buffers (openclsim.c:741-809). The kernel entry point must be named
+ * "mkg_tissue_step".
+ */
+int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
+               mkg_sim **sim);
+
+/* Frees everything; safe on NULL and on a handle after any error.
+ * Replaces sim_clean (openclsim.c:216-292). */
+void mkg_destroy(mkg_sim *sim);
+
+/* Last error message for this handle, or for the calling thread when sim is
+ * NULL. Never returns NULL. */
+const char *mkg_last_error(const mkg_sim *sim);
+
+/* Cell state, AoS doubles, n = nx*ny*n_state (state_in, openclsim.c:512-521;
+ * state_out, openclsim.c:1185-1190). */
+int mkg_set_state(mkg_sim *sim, const double *state, int64_t n);
+int mkg_get_state(mkg_sim *sim, double *state, int64_t n);
+
+/* Scalar fields, cell-major interleaved: field_data[cell*n_field + k]
+ * (openclsim.py:1082-1089, openclsim.cl:201). n = nx*ny*n_field. */
+int mkg_set_fields(mkg_sim *sim, const double *field_data, int64_t n);
+
+/* Homogeneous conductances gx, gy (sim_init gx/gy, openclsim.c:395-396). */
+int mkg_set_conductance(mkg_sim *sim, double gx, double gy);
+
+/* Per-edge conductances in the reference layout: gx has ny*(nx-1) entries,
+ * gy has (ny-1)*nx (openclsim.py:1380-1384, openclsim.cl:452-487). */
+int mkg_set_conductance_field(mkg_sim *sim, const double *gx, int64_t ngx,
+                              const double *gy, int64_t ngy);
+
+/* Connections (cell1[i], cell2[i], g[i]) as validated by
+ * SimulationOpenCL.set_connections (openclsim.py:1387-1449). Stored as a
+ * per-cell neighbour list so each cell sums its currents in a fixed order. */
+int mkg_set_connections(mkg_sim *sim, const int64_t *cell1,
+                        const int64_t *cell2, const double *g, int64_t n);
+
+/* Paced cells (calculate_pacing, openclsim.cl:249-280). */
+int mkg_set_pacing_mode(mkg_sim *sim, int32_t mode);
+int mkg_set_paced_rect(mkg_sim *sim, int64_t nx, int64_t ny, int64_t x,
+                       int64_t y);
+int mkg_set_paced_list(mkg_sim *sim, const int64_t *cells, int64_t n);
+
+/* Protocol events, n rows of (level, start, duration, period, multiplier),
+ * the attributes ESys_Populate reads (pacing.h:340-470). */
+int mkg_set_protocol(mkg_sim *sim, const double *events, int64_t n);
+
+/* Logged per-cell columns: column j records item[j] of cell[j]. item is a
+ * state index, MKG_ITEM_IDIFF or MKG_ITEM_INTER (openclsim.c:941-1001).
+ * nan_check = 1 applies the reference's NaN halt, which looks at the first
+ * state entry at every log point when states are logged (openclsim.c:1080-
+ * 1089). */
+int mkg_set_log(mkg_sim *sim, const int32_t *item, const int64_t *cell,
+                int64_t ncol, int32_t nan_check);
+
+/* Starts a run over [tmin, tmax) with the given default step and log
+ * interval (the scalar arguments of sim_init, openclsim.c:397-403, and its
+ * pacing set-up, openclsim.c:488-496). */
+int mkg_run_begin(mkg_sim *sim, double tmin, double tmax, double default_dt,
+                  double log_interval);
+
+/*
+ * Advances the run by at most max_steps steps (sim_step, openclsim.c:1036-
+ * 1211, with the reference's step-size schedule, pacing and logging). Sets
+ * *t_out to the engine time reached and *rows_out to the log rows produced.
+ * Returns MKG_OK while the run continues, MKG_DONE at tmax, MKG_HALT_NAN
+ * after the reference's NaN halt, or a negative error.
+ */
+int mkg_run_chunk(mkg_sim *sim, int64_t max_steps, double *t_out,
+                  int64_t *rows_out);
+
+/* Copies the rows of the last chunk: time[r], pace[r] (the engine values
+ * cast to the simulation precision, openclsim.c:1063, 1148-1155) and
+ * values[r*ncol + j]. Any pointer may be NULL. */
+int mkg_read_log(mkg_sim *sim, double *time, double *pace, double *values,
+                 int64_t rows);
+
+/* Launch tuning: steps fused into one launch (0 = automatic) and blocks per
+ * SM for the persistent grid (0 = occupancy maximum). */
+int mkg_set_tuning(mkg_sim *sim, int32_t steps_per_launch,
+                   int32_t blocks_per_sm);
+
+/* Timing and counters of the last chunk: device milliseconds spent in
+ * step kernels, number of kernel launches and cell-steps computed. */
+int mkg_last_stats(const mkg_sim *sim, double *kernel_ms, int64_t *launches,
+                   int64_t *cell_steps);
+
+/*
+ * Host-only view of the step schedule that mkg_run_chunk follows: the first
+ * at most max_steps steps of a run over [tmin, tmax) with the given protocol
+ * (events as in mkg_set_protocol). Writes t, dt, pace and log (0/1) per step
+ * and returns the number of steps (or a negative error). Needs no GPU; it
+ * exists so the schedule can be checked against the reference's
+ * (openclsim.c:1051-1162) on any machine.
+ */
+int64_t mkg_schedule_preview(const double *events, int64_t n_events,
+                             double tmin, double tmax, double default_dt,
+                             double log_interval, int64_t max_steps,
+                             double *t, double *dt, double *pace,
+                             int32_t *log);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MKG_TISSUE_H */

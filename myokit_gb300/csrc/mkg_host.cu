@@ -1,0 +1,1024 @@
+/*
+ * mkg_host.cu -- host library behind include/mkg_tissue.h.
+ *
+ * Replaces the generated CPython module of myokit's SimulationOpenCL
+ * (myokit/_sim/openclsim.c) and its OpenCL runtime calls (myokit/_sim/mcl.h):
+ *
+ *   openclsim.c sim_init  -> mkg_create + mkg_set_* + mkg_run_begin
+ *   openclsim.c sim_step  -> mkg_run_chunk (+ mkg_read_log)
+ *   openclsim.c sim_clean -> mkg_destroy
+ *   clBuildProgram        -> mkg_compile (NVRTC, sm_103a cubin)
+ *
+ * Where the reference enqueues two kernels per step and copies the whole
+ * state to the host at every log point, this library uploads a schedule of
+ * many steps, runs them in one cooperative launch of the generated fused
+ * kernel, and copies back only the logged columns of the logged steps.
+ *
+ * Also holds the fixed (not generated) kernels: AoS <-> SoA state
+ * conversion and precision conversion of per-edge conductances.
+ */
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mkg_tissue.h"
+#include "mkg_kernel_abi.h"
+#include "mkg_pacing.h"
+
+namespace {
+
+thread_local std::string g_thread_error;
+
+/* ------------------------------------------------------------------------ */
+/* Fixed device kernels                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* AoS doubles [ncell][nvar] -> SoA Real [nvar][pitch]; variable skip_var
+ * (if >= 0) goes to alt instead (the V ping-pong plane). */
+template <typename Real>
+__global__ void k_aos_to_soa(const double *__restrict__ in, Real *out,
+                             long long ncell, int nvar, long long pitch,
+                             int skip_var, Real *alt)
+{
+    const long long n = ncell * nvar;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+         i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int s = (int)(i / ncell);
+        const long long c = i - (long long)s * ncell;
+        const Real v = (Real)in[c * nvar + s];
+        if (s == skip_var) alt[c] = v;
+        else out[(long long)s * pitch + c] = v;
+    }
+}
+
+/* SoA Real -> AoS doubles, the inverse of k_aos_to_soa. */
+template <typename Real>
+__global__ void k_soa_to_aos(const Real *__restrict__ in, double *out,
+                             long long ncell, int nvar, long long pitch,
+                             int skip_var, const Real *alt)
+{
+    const long long n = ncell * nvar;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+         i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int s = (int)(i / ncell);
+        const long long c = i - (long long)s * ncell;
+        const Real v = (s == skip_var) ? alt[c] : in[(long long)s * pitch + c];
+        out[c * nvar + s] = (double)v;
+    }
+}
+
+template <typename Real>
+__global__ void k_convert(const double *__restrict__ in, Real *out,
+                          long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+         i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (Real)in[i];
+}
+
+template <typename Real>
+__global__ void k_log_to_double(const Real *__restrict__ in, double *out,
+                                long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+         i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+int grid_for(long long n)
+{
+    long long b = (n + 255) / 256;
+    if (b < 1) b = 1;
+    if (b > 152 * 32) b = 152 * 32;
+    return (int)b;
+}
+
+}  // namespace
+
+/* ------------------------------------------------------------------------ */
+/* Simulation handle                                                        */
+/* ------------------------------------------------------------------------ */
+
+struct mkg_sim {
+    mkg_config cfg;
+    std::string error;
+    int real;                 /* bytes per Real */
+    long long ncell, pitch;
+
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t kernel = nullptr;
+    int occ_blocks = 1;       /* co-resident blocks per SM */
+    int num_sms = 1;
+
+    /* device buffers */
+    void *d_state = nullptr;  /* Real[n_state][pitch] */
+    void *d_vbuf = nullptr;   /* Real[2][pitch] */
+    void *d_field = nullptr;  /* Real[n_field][pitch] */
+    void *d_gx = nullptr, *d_gy = nullptr;
+    int *d_nbr_ptr = nullptr, *d_nbr_idx = nullptr;
+    void *d_nbr_g = nullptr;
+    unsigned int *d_pace_bits = nullptr;
+    int *d_log_items = nullptr, *d_log_cols = nullptr;
+    void *d_log = nullptr;
+    double *d_log_dbl = nullptr;
+    mkg_step *d_steps = nullptr;
+    mkg_status *d_status = nullptr;
+    double *d_stage = nullptr;   /* staging for double uploads */
+    size_t stage_bytes = 0;
+
+    /* pinned host buffers */
+    mkg_step *h_steps = nullptr;
+    mkg_status *h_status = nullptr;
+    double *h_log = nullptr;
+    std::vector<double> h_time, h_pace, h_tend;
+
+    int v_sel = 0;
+    double gx = 0, gy = 0;
+    int pace_mode = MKG_PACE_NONE;
+    long long px0 = 0, px1 = 0, py0 = 0, py1 = 0;
+    int n_log_items = 0;
+    int log_ncol = 0;
+    int nan_check = 0;
+    int64_t cap_steps = 0;    /* schedule capacity */
+    int64_t cap_rows = 0;     /* log row capacity */
+    int64_t last_rows = 0;
+    int steps_per_launch = 0;
+    int blocks_per_sm = 0;
+    long long timeout_ns = 2000000000LL;
+
+    mkg::Pacer pacer;
+    mkg::Schedule sched;
+    bool running = false;
+    bool halted = false;
+
+    double last_ms = 0;
+    int64_t last_launches = 0, last_cell_steps = 0;
+};
+
+namespace {
+
+int set_err(mkg_sim *s, int code, const char *fmt, ...)
+{
+    char buf[2048];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (s) s->error = buf;
+    else g_thread_error = buf;
+    return code;
+}
+
+#define CK(sim, call)                                                       \
+    do {                                                                    \
+        cudaError_t e_ = (call);                                            \
+        if (e_ != cudaSuccess)                                              \
+            return set_err(sim, MKG_ERR_CUDA, "%s failed: %s (%s:%d)",      \
+                           #call, cudaGetErrorString(e_), __FILE__,        \
+                           __LINE__);                                       \
+    } while (0)
+
+template <typename T>
+void dfree(T *&p)
+{
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+
+int ensure_stage(mkg_sim *s, size_t bytes)
+{
+    if (bytes <= s->stage_bytes) return MKG_OK;
+    dfree(s->d_stage);
+    s->stage_bytes = 0;
+    CK(s, cudaMalloc((void **)&s->d_stage, bytes));
+    s->stage_bytes = bytes;
+    return MKG_OK;
+}
+
+int ensure_schedule(mkg_sim *s, int64_t steps, int64_t rows)
+{
+    if (steps > s->cap_steps) {
+        dfree(s->d_steps);
+        if (s->h_steps) cudaFreeHost(s->h_steps);
+        s->h_steps = nullptr;
+        s->cap_steps = 0;
+        CK(s, cudaMalloc((void **)&s->d_steps, steps * sizeof(mkg_step)));
+        CK(s, cudaMallocHost((void **)&s->h_steps, steps * sizeof(mkg_step)));
+        s->h_tend.resize(steps);
+        s->cap_steps = steps;
+    }
+    if (rows > s->cap_rows) {
+        dfree(s->d_log);
+        dfree(s->d_log_dbl);
+        if (s->h_log) cudaFreeHost(s->h_log);
+        s->h_log = nullptr;
+        s->cap_rows = 0;
+        const size_t n = (size_t)rows * (size_t)std::max(s->log_ncol, 1);
+        CK(s, cudaMalloc(&s->d_log, n * s->real));
+        CK(s, cudaMalloc((void **)&s->d_log_dbl, n * sizeof(double)));
+        CK(s, cudaMallocHost((void **)&s->h_log, n * sizeof(double)));
+        s->h_time.resize(rows);
+        s->h_pace.resize(rows);
+        s->cap_rows = rows;
+    }
+    return MKG_OK;
+}
+
+template <typename Real>
+int upload_soa(mkg_sim *s, const double *aos, int nvar, void *dst,
+               int skip_var, void *alt)
+{
+    const size_t bytes = (size_t)s->ncell * nvar * sizeof(double);
+    int r = ensure_stage(s, bytes);
+    if (r) return r;
+    CK(s, cudaMemcpyAsync(s->d_stage, aos, bytes, cudaMemcpyHostToDevice,
+                          s->stream));
+    k_aos_to_soa<Real><<<grid_for(s->ncell * nvar), 256, 0, s->stream>>>(
+        s->d_stage, (Real *)dst, s->ncell, nvar, s->pitch, skip_var,
+        (Real *)alt);
+    CK(s, cudaGetLastError());
+    CK(s, cudaStreamSynchronize(s->stream));
+    return MKG_OK;
+}
+
+template <typename Real>
+int download_soa(mkg_sim *s, double *aos, int nvar, const void *src,
+                 int skip_var, const void *alt)
+{
+    const size_t bytes = (size_t)s->ncell * nvar * sizeof(double);
+    int r = ensure_stage(s, bytes);
+    if (r) return r;
+    k_soa_to_aos<Real><<<grid_for(s->ncell * nvar), 256, 0, s->stream>>>(
+        (const Real *)src, s->d_stage, s->ncell, nvar, s->pitch, skip_var,
+        (const Real *)alt);
+    CK(s, cudaGetLastError());
+    CK(s, cudaMemcpyAsync(aos, s->d_stage, bytes, cudaMemcpyDeviceToHost,
+                          s->stream));
+    CK(s, cudaStreamSynchronize(s->stream));
+    return MKG_OK;
+}
+
+template <typename Real>
+int upload_real(mkg_sim *s, const double *src, long long n, void *dst)
+{
+    if (n <= 0) return MKG_OK;
+    int r = ensure_stage(s, (size_t)n * sizeof(double));
+    if (r) return r;
+    CK(s, cudaMemcpyAsync(s->d_stage, src, n * sizeof(double),
+                          cudaMemcpyHostToDevice, s->stream));
+    k_convert<Real><<<grid_for(n), 256, 0, s->stream>>>(s->d_stage,
+                                                       (Real *)dst, n);
+    CK(s, cudaGetLastError());
+    CK(s, cudaStreamSynchronize(s->stream));
+    return MKG_OK;
+}
+
+bool diffusion_on(const mkg_sim *s) { return s->cfg.diffusion != MKG_DIFF_NONE; }
+
+int pacer_err(mkg_sim *s, int st)
+{
+    if (st == mkg::PACER_SIMULTANEOUS_EVENT)
+        return set_err(s, MKG_ERR_SIMULTANEOUS,
+                       "E-Pacing error: Event scheduled or re-occuring at the"
+                       " same time as another event.");
+    if (st == mkg::PACER_NEGATIVE_TIME_INCREMENT)
+        return set_err(s, MKG_ERR_PACING,
+                       "E-Pacing error: New time is before current time.");
+    if (st == mkg::PACER_NON_ZERO_MULTIPLIER)
+        return set_err(s, MKG_ERR_PACING,
+                       "E-Pacing error: Non-zero multiplier found for"
+                       " non-periodic stimulus.");
+    if (st == mkg::PACER_NEGATIVE_PERIOD)
+        return set_err(s, MKG_ERR_PACING,
+                       "E-Pacing error: Pacing event period cannot be"
+                       " negative.");
+    if (st == mkg::PACER_NEGATIVE_MULTIPLIER)
+        return set_err(s, MKG_ERR_PACING,
+                       "E-Pacing error: Pacing event multiplier cannot be"
+                       " negative.");
+    return set_err(s, MKG_ERR_PACING, "E-Pacing error: Unlisted error %d",
+                   st);
+}
+
+}  // namespace
+
+/* ------------------------------------------------------------------------ */
+/* C ABI                                                                    */
+/* ------------------------------------------------------------------------ */
+
+extern "C" {
+
+const char *mkg_last_error(const mkg_sim *sim)
+{
+    if (sim) return sim->error.c_str();
+    return g_thread_error.c_str();
+}
+
+void mkg_free(void *ptr) { free(ptr); }
+
+int mkg_compile(const char *source, const char *name,
+                const char *const *options, int n_options, void **cubin,
+                size_t *cubin_size, char **log)
+{
+    if (!source || !cubin || !cubin_size)
+        return set_err(nullptr, MKG_ERR_ARG, "mkg_compile: null argument");
+    *cubin = nullptr;
+    *cubin_size = 0;
+    if (log) *log = nullptr;
+    nvrtcProgram prog;
+    nvrtcResult r = nvrtcCreateProgram(&prog, source,
+                                       name ? name : "mkg_tissue.cu", 0,
+                                       nullptr, nullptr);
+    if (r != NVRTC_SUCCESS)
+        return set_err(nullptr, MKG_ERR_COMPILE, "nvrtcCreateProgram: %s",
+                       nvrtcGetErrorString(r));
+    r = nvrtcCompileProgram(prog, n_options, options);
+    size_t log_size = 0;
+    nvrtcGetProgramLogSize(prog, &log_size);
+    std::string text(log_size > 0 ? log_size : 1, '\0');
+    if (log_size > 1) nvrtcGetProgramLog(prog, &text[0]);
+    if (log) {
+        *log = (char *)malloc(text.size() + 1);
+        if (*log) memcpy(*log, text.c_str(), text.size() + 1);
+    }
+    if (r != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        return set_err(nullptr, MKG_ERR_COMPILE,
+                       "Kernel failed to compile (%s):\n%s",
+                       nvrtcGetErrorString(r), text.c_str());
+    }
+    size_t n = 0;
+    r = nvrtcGetCUBINSize(prog, &n);
+    if (r != NVRTC_SUCCESS || n == 0) {
+        nvrtcDestroyProgram(&prog);
+        return set_err(nullptr, MKG_ERR_COMPILE, "no cubin produced");
+    }
+    void *out = malloc(n);
+    if (!out) {
+        nvrtcDestroyProgram(&prog);
+        return set_err(nullptr, MKG_ERR_NOMEM, "out of host memory");
+    }
+    nvrtcGetCUBIN(prog, (char *)out);
+    nvrtcDestroyProgram(&prog);
+    *cubin = out;
+    *cubin_size = n;
+    return MKG_OK;
+}
+
+void mkg_destroy(mkg_sim *s)
+{
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    dfree(s->d_state);
+    dfree(s->d_vbuf);
+    dfree(s->d_field);
+    dfree(s->d_gx);
+    dfree(s->d_gy);
+    dfree(s->d_nbr_ptr);
+    dfree(s->d_nbr_idx);
+    dfree(s->d_nbr_g);
+    dfree(s->d_pace_bits);
+    dfree(s->d_log_items);
+    dfree(s->d_log_cols);
+    dfree(s->d_log);
+    dfree(s->d_log_dbl);
+    dfree(s->d_steps);
+    dfree(s->d_status);
+    dfree(s->d_stage);
+    if (s->h_steps) cudaFreeHost(s->h_steps);
+    if (s->h_status) cudaFreeHost(s->h_status);
+    if (s->h_log) cudaFreeHost(s->h_log);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->lib) cudaLibraryUnload(s->lib);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
+               mkg_sim **out)
+{
+    if (!cfg || !cubin || !cubin_size || !out)
+        return set_err(nullptr, MKG_ERR_ARG, "mkg_create: null argument");
+    *out = nullptr;
+    if (cfg->nx < 1 || cfg->ny < 1)
+        return set_err(nullptr, MKG_ERR_ARG,
+                       "The number of cells in any direction must be at"
+                       " least 1.");
+    if (cfg->real_bytes != 4 && cfg->real_bytes != 8)
+        return set_err(nullptr, MKG_ERR_ARG,
+                       "Only single and double precision are supported.");
+    if (cfg->n_state < 1 || cfg->n_field < 0 || cfg->n_inter < 0)
+        return set_err(nullptr, MKG_ERR_ARG, "invalid variable counts");
+    if (cfg->diffusion < MKG_DIFF_NONE || cfg->diffusion > MKG_DIFF_CONN)
+        return set_err(nullptr, MKG_ERR_ARG, "invalid diffusion mode");
+    if (cfg->diffusion != MKG_DIFF_NONE &&
+        (cfg->i_vm < 0 || cfg->i_vm >= cfg->n_state))
+        return set_err(nullptr, MKG_ERR_ARG, "invalid membrane potential index");
+    if (cfg->block_x < 1 || cfg->block_y < 1 ||
+        cfg->block_x * cfg->block_y > 1024)
+        return set_err(nullptr, MKG_ERR_ARG, "invalid block shape");
+    if (!cfg->two_d && cfg->block_y != 1)
+        return set_err(nullptr, MKG_ERR_ARG, "flat kernels need block_y 1");
+    if (!cfg->two_d && cfg->ny != 1 && cfg->diffusion != MKG_DIFF_NONE)
+        return set_err(nullptr, MKG_ERR_ARG, "2D diffusion needs two_d");
+
+    mkg_sim *s = new mkg_sim();
+    s->cfg = *cfg;
+    s->real = cfg->real_bytes;
+    s->ncell = cfg->nx * cfg->ny;
+    s->pitch = (s->ncell + 31) / 32 * 32;
+    s->pace_mode = cfg->diffusion == MKG_DIFF_NONE ? MKG_PACE_ALL
+                                                   : MKG_PACE_NONE;
+#define CKC(call)                                                           \
+    do {                                                                    \
+        cudaError_t e_ = (call);                                            \
+        if (e_ != cudaSuccess) {                                            \
+            set_err(nullptr, MKG_ERR_CUDA, "%s failed: %s", #call,          \
+                    cudaGetErrorString(e_));                                \
+            mkg_destroy(s);                                                 \
+            return MKG_ERR_CUDA;                                            \
+        }                                                                   \
+    } while (0)
+    CKC(cudaSetDevice(cfg->device));
+    CKC(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    CKC(cudaEventCreate(&s->ev0));
+    CKC(cudaEventCreate(&s->ev1));
+    CKC(cudaLibraryLoadData(&s->lib, cubin, nullptr, nullptr, 0, nullptr,
+                            nullptr, 0));
+    CKC(cudaLibraryGetKernel(&s->kernel, s->lib, "mkg_tissue_step"));
+    CKC(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount,
+                               cfg->device));
+    CKC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &s->occ_blocks, (const void *)s->kernel,
+        cfg->block_x * cfg->block_y, 0));
+    if (s->occ_blocks < 1) {
+        set_err(nullptr, MKG_ERR_CUDA,
+                "the generated kernel cannot be resident on an SM");
+        mkg_destroy(s);
+        return MKG_ERR_CUDA;
+    }
+
+    const size_t plane = (size_t)s->pitch * s->real;
+    CKC(cudaMalloc(&s->d_state, plane * cfg->n_state));
+    CKC(cudaMemsetAsync(s->d_state, 0, plane * cfg->n_state, s->stream));
+    CKC(cudaMalloc(&s->d_vbuf, plane * 2));
+    CKC(cudaMemsetAsync(s->d_vbuf, 0, plane * 2, s->stream));
+    if (cfg->n_field > 0) {
+        CKC(cudaMalloc(&s->d_field, plane * cfg->n_field));
+        CKC(cudaMemsetAsync(s->d_field, 0, plane * cfg->n_field, s->stream));
+    }
+    CKC(cudaMalloc((void **)&s->d_status, sizeof(mkg_status)));
+    CKC(cudaMallocHost((void **)&s->h_status, sizeof(mkg_status)));
+    CKC(cudaStreamSynchronize(s->stream));
+#undef CKC
+    *out = s;
+    return MKG_OK;
+}
+
+int mkg_set_state(mkg_sim *s, const double *state, int64_t n)
+{
+    if (!s || !state) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (n != s->ncell * s->cfg.n_state)
+        return set_err(s, MKG_ERR_ARG,
+                       "'state_in' must have size nx * ny * n_states.");
+    const int skip = diffusion_on(s) ? s->cfg.i_vm : -1;
+    void *alt = (char *)s->d_vbuf + (size_t)s->v_sel * s->pitch * s->real;
+    if (s->real == 4)
+        return upload_soa<float>(s, state, s->cfg.n_state, s->d_state, skip,
+                                 alt);
+    return upload_soa<double>(s, state, s->cfg.n_state, s->d_state, skip,
+                              alt);
+}
+
+int mkg_get_state(mkg_sim *s, double *state, int64_t n)
+{
+    if (!s || !state) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (n != s->ncell * s->cfg.n_state)
+        return set_err(s, MKG_ERR_ARG,
+                       "'state_out' must have size nx * ny * n_states.");
+    const int skip = diffusion_on(s) ? s->cfg.i_vm : -1;
+    const void *alt =
+        (const char *)s->d_vbuf + (size_t)s->v_sel * s->pitch * s->real;
+    if (s->real == 4)
+        return download_soa<float>(s, state, s->cfg.n_state, s->d_state, skip,
+                                   alt);
+    return download_soa<double>(s, state, s->cfg.n_state, s->d_state, skip,
+                                alt);
+}
+
+int mkg_set_fields(mkg_sim *s, const double *field_data, int64_t n)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (n != s->ncell * s->cfg.n_field)
+        return set_err(s, MKG_ERR_ARG,
+                       "field data must have nx * ny * n_field entries");
+    if (n == 0) return MKG_OK;
+    if (!field_data) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (s->real == 4)
+        return upload_soa<float>(s, field_data, s->cfg.n_field, s->d_field,
+                                 -1, nullptr);
+    return upload_soa<double>(s, field_data, s->cfg.n_field, s->d_field, -1,
+                              nullptr);
+}
+
+int mkg_set_conductance(mkg_sim *s, double gx, double gy)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (gx < 0) return set_err(s, MKG_ERR_ARG, "Invalid conductance gx=%g", gx);
+    if (gy < 0) return set_err(s, MKG_ERR_ARG, "Invalid conductance gy=%g", gy);
+    s->gx = gx;
+    s->gy = gy;
+    return MKG_OK;
+}
+
+int mkg_set_conductance_field(mkg_sim *s, const double *gx, int64_t ngx,
+                              const double *gy, int64_t ngy)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    const long long nx = s->cfg.nx, ny = s->cfg.ny;
+    if (ngx != ny * (nx - 1))
+        return set_err(s, MKG_ERR_ARG, "gx must have ny * (nx - 1) entries");
+    if (ngy != (ny - 1) * nx)
+        return set_err(s, MKG_ERR_ARG, "gy must have (ny - 1) * nx entries");
+    for (int64_t i = 0; i < ngx; ++i)
+        if (!(gx[i] >= 0))
+            return set_err(s, MKG_ERR_ARG,
+                           "The argument `gx` can not contain negative"
+                           " values.");
+    for (int64_t i = 0; i < ngy; ++i)
+        if (!(gy[i] >= 0))
+            return set_err(s, MKG_ERR_ARG,
+                           "The argument `gy` can not contain negative"
+                           " values.");
+    dfree(s->d_gx);
+    dfree(s->d_gy);
+    CK(s, cudaMalloc(&s->d_gx, std::max<int64_t>(ngx, 1) * s->real));
+    CK(s, cudaMalloc(&s->d_gy, std::max<int64_t>(ngy, 1) * s->real));
+    int r;
+    if (s->real == 4) {
+        if ((r = upload_real<float>(s, gx, ngx, s->d_gx))) return r;
+        if ((r = upload_real<float>(s, gy, ngy, s->d_gy))) return r;
+    } else {
+        if ((r = upload_real<double>(s, gx, ngx, s->d_gx))) return r;
+        if ((r = upload_real<double>(s, gy, ngy, s->d_gy))) return r;
+    }
+    return MKG_OK;
+}
+
+int mkg_set_connections(mkg_sim *s, const int64_t *c1, const int64_t *c2,
+                        const double *g, int64_t n)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (n < 0 || (n > 0 && (!c1 || !c2 || !g)))
+        return set_err(s, MKG_ERR_ARG, "invalid connection arrays");
+    const long long nc = s->ncell;
+    std::vector<int> deg(nc + 1, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        if (c1[i] < 0 || c2[i] < 0 || c1[i] >= nc || c2[i] >= nc ||
+            c1[i] == c2[i])
+            return set_err(s, MKG_ERR_ARG,
+                           "Invalid connection: (%lld, %lld, %g)",
+                           (long long)c1[i], (long long)c2[i], g[i]);
+        if (!(g[i] >= 0))
+            return set_err(s, MKG_ERR_ARG, "Invalid conductance: %g", g[i]);
+        deg[c1[i]]++;
+        deg[c2[i]]++;
+    }
+    std::vector<int> ptr(nc + 1, 0);
+    for (long long i = 0; i < nc; ++i) ptr[i + 1] = ptr[i] + deg[i];
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    std::vector<int> idx(std::max<int64_t>(2 * n, 1));
+    std::vector<double> gg(std::max<int64_t>(2 * n, 1));
+    /* Each cell's list keeps the order of the connection list. */
+    for (int64_t i = 0; i < n; ++i) {
+        const int a = (int)c1[i], b = (int)c2[i];
+        idx[fill[a]] = b;
+        gg[fill[a]++] = g[i];
+        idx[fill[b]] = a;
+        gg[fill[b]++] = g[i];
+    }
+    dfree(s->d_nbr_ptr);
+    dfree(s->d_nbr_idx);
+    dfree(s->d_nbr_g);
+    CK(s, cudaMalloc((void **)&s->d_nbr_ptr, (nc + 1) * sizeof(int)));
+    CK(s, cudaMalloc((void **)&s->d_nbr_idx, idx.size() * sizeof(int)));
+    CK(s, cudaMalloc(&s->d_nbr_g, gg.size() * s->real));
+    CK(s, cudaMemcpyAsync(s->d_nbr_ptr, ptr.data(), (nc + 1) * sizeof(int),
+                          cudaMemcpyHostToDevice, s->stream));
+    CK(s, cudaMemcpyAsync(s->d_nbr_idx, idx.data(), idx.size() * sizeof(int),
+                          cudaMemcpyHostToDevice, s->stream));
+    CK(s, cudaStreamSynchronize(s->stream));
+    if (s->real == 4)
+        return upload_real<float>(s, gg.data(), (long long)gg.size(), s->d_nbr_g);
+    return upload_real<double>(s, gg.data(), (long long)gg.size(), s->d_nbr_g);
+}
+
+int mkg_set_pacing_mode(mkg_sim *s, int32_t mode)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (mode < MKG_PACE_ALL || mode > MKG_PACE_NONE)
+        return set_err(s, MKG_ERR_ARG, "invalid pacing mode");
+    s->pace_mode = mode;
+    return MKG_OK;
+}
+
+int mkg_set_paced_rect(mkg_sim *s, int64_t nx, int64_t ny, int64_t x,
+                       int64_t y)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    s->px0 = x;
+    s->px1 = x + nx;
+    s->py0 = y;
+    s->py1 = y + ny;
+    s->pace_mode = MKG_PACE_RECT;
+    return MKG_OK;
+}
+
+int mkg_set_paced_list(mkg_sim *s, const int64_t *cells, int64_t n)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    const long long words = (s->ncell + 31) / 32;
+    std::vector<unsigned int> bits(words, 0u);
+    for (int64_t i = 0; i < n; ++i) {
+        if (cells[i] < 0 || cells[i] >= s->ncell)
+            return set_err(s, MKG_ERR_ARG, "Cell index out of range: %lld.",
+                           (long long)cells[i]);
+        bits[cells[i] >> 5] |= 1u << (cells[i] & 31);
+    }
+    dfree(s->d_pace_bits);
+    CK(s, cudaMalloc((void **)&s->d_pace_bits, words * sizeof(unsigned int)));
+    CK(s, cudaMemcpyAsync(s->d_pace_bits, bits.data(),
+                          words * sizeof(unsigned int),
+                          cudaMemcpyHostToDevice, s->stream));
+    CK(s, cudaStreamSynchronize(s->stream));
+    s->pace_mode = n > 0 ? MKG_PACE_LIST : MKG_PACE_NONE;
+    return MKG_OK;
+}
+
+int mkg_set_protocol(mkg_sim *s, const double *events, int64_t n)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (n < 0 || (n > 0 && !events))
+        return set_err(s, MKG_ERR_ARG, "invalid event array");
+    const int st = s->pacer.populate(events, n);
+    if (st != mkg::PACER_OK) return pacer_err(s, st);
+    return MKG_OK;
+}
+
+int mkg_set_log(mkg_sim *s, const int32_t *item, const int64_t *cell,
+                int64_t ncol, int32_t nan_check)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (ncol < 0 || (ncol > 0 && (!item || !cell)) || ncol > INT_MAX)
+        return set_err(s, MKG_ERR_ARG, "invalid log columns");
+    const int n_items_total = s->cfg.n_state + 1 + s->cfg.n_inter;
+    std::vector<int> slot_of(n_items_total, -1);
+    std::vector<int> items;
+    for (int64_t j = 0; j < ncol; ++j) {
+        if (item[j] < 0 || item[j] >= n_items_total)
+            return set_err(s, MKG_ERR_ARG, "invalid log item %d", item[j]);
+        if (item[j] == s->cfg.n_state && !diffusion_on(s))
+            return set_err(s, MKG_ERR_ARG,
+                           "diffusion current logged without diffusion");
+        if (cell[j] < 0 || cell[j] >= s->ncell)
+            return set_err(s, MKG_ERR_ARG, "invalid log cell %lld",
+                           (long long)cell[j]);
+        if (slot_of[item[j]] < 0) {
+            slot_of[item[j]] = (int)items.size();
+            items.push_back(item[j]);
+        }
+    }
+    std::vector<int> cols((size_t)std::max<size_t>(items.size(), 1) *
+                          s->pitch, -1);
+    for (int64_t j = 0; j < ncol; ++j)
+        cols[(size_t)slot_of[item[j]] * s->pitch + cell[j]] = (int)j;
+    dfree(s->d_log_items);
+    dfree(s->d_log_cols);
+    CK(s, cudaMalloc((void **)&s->d_log_items,
+                     std::max<size_t>(items.size(), 1) * sizeof(int)));
+    CK(s, cudaMalloc((void **)&s->d_log_cols, cols.size() * sizeof(int)));
+    if (!items.empty())
+        CK(s, cudaMemcpyAsync(s->d_log_items, items.data(),
+                              items.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, s->stream));
+    CK(s, cudaMemcpyAsync(s->d_log_cols, cols.data(),
+                          cols.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          s->stream));
+    CK(s, cudaStreamSynchronize(s->stream));
+    s->n_log_items = (int)items.size();
+    /* A new column count invalidates the log buffers. */
+    if ((int)ncol != s->log_ncol) {
+        dfree(s->d_log);
+        dfree(s->d_log_dbl);
+        if (s->h_log) cudaFreeHost(s->h_log);
+        s->h_log = nullptr;
+        s->cap_rows = 0;
+    }
+    s->log_ncol = (int)ncol;
+    s->nan_check = nan_check ? 1 : 0;
+    return MKG_OK;
+}
+
+int mkg_set_tuning(mkg_sim *s, int32_t steps_per_launch,
+                   int32_t blocks_per_sm)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (steps_per_launch < 0 || blocks_per_sm < 0)
+        return set_err(s, MKG_ERR_ARG, "invalid tuning");
+    s->steps_per_launch = steps_per_launch;
+    s->blocks_per_sm = blocks_per_sm;
+    return MKG_OK;
+}
+
+int mkg_run_begin(mkg_sim *s, double tmin, double tmax, double default_dt,
+                  double log_interval)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (!(default_dt > 0))
+        return set_err(s, MKG_ERR_ARG, "Step size must be greater than zero.");
+    if (!(log_interval > 0))
+        return set_err(s, MKG_ERR_ARG, "log interval must be positive");
+    if (diffusion_on(s) && s->cfg.diffusion == MKG_DIFF_HETERO &&
+        (!s->d_gx || !s->d_gy))
+        return set_err(s, MKG_ERR_ORDER, "conductance field not set");
+    if (s->cfg.diffusion == MKG_DIFF_CONN && !s->d_nbr_ptr)
+        return set_err(s, MKG_ERR_ORDER, "connections not set");
+    if (s->pace_mode == MKG_PACE_LIST && !s->d_pace_bits)
+        return set_err(s, MKG_ERR_ORDER, "paced cell list not set");
+    if (!s->d_log_cols) {
+        int r = mkg_set_log(s, nullptr, nullptr, 0, 0);
+        if (r) return r;
+    }
+    const int st = s->sched.begin(s->pacer, tmin, tmax, default_dt,
+                                  log_interval);
+    if (st != mkg::PACER_OK) return pacer_err(s, st);
+    s->running = true;
+    s->halted = false;
+    s->last_rows = 0;
+    return MKG_OK;
+}
+
+int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
+                  int64_t *rows_out)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (rows_out) *rows_out = 0;
+    if (!s->running)
+        return set_err(s, MKG_ERR_ORDER, "mkg_run_chunk before mkg_run_begin");
+    if (max_steps < 1) return set_err(s, MKG_ERR_ARG, "max_steps < 1");
+    s->last_ms = 0;
+    s->last_launches = 0;
+    s->last_cell_steps = 0;
+    s->last_rows = 0;
+    if (s->sched.done()) {
+        if (t_out) *t_out = s->sched.time();
+        s->running = false;
+        return MKG_DONE;
+    }
+
+    /* Log rows that fit a 256 MiB buffer, at least 16. */
+    const int64_t ncol = std::max(s->log_ncol, 1);
+    int64_t row_cap = (int64_t)(256ll << 20) / (ncol * 8);
+    row_cap = std::max<int64_t>(16, std::min<int64_t>(row_cap, max_steps));
+    int r = ensure_schedule(s, max_steps, row_cap);
+    if (r) return r;
+
+    /* Host schedule for this chunk (openclsim.c:1051-1162). */
+    int64_t n = 0, rows = 0;
+    while (n < max_steps && !s->sched.done()) {
+        if (s->sched.next_logs() && rows == row_cap) break;
+        mkg::StepRecord rec;
+        const int st = s->sched.next(&rec);
+        if (st != mkg::PACER_OK) {
+            s->running = false;
+            return pacer_err(s, st);
+        }
+        mkg_step &h = s->h_steps[n];
+        h.t = rec.t;
+        h.dt = rec.dt;
+        h.pace = rec.pace;
+        h.pad = 0;
+        if (rec.log) {
+            h.log_row = (int)rows;
+            if (s->real == 4) {
+                s->h_time[rows] = (double)(float)rec.t;
+                s->h_pace[rows] = (double)(float)rec.pace;
+            } else {
+                s->h_time[rows] = rec.t;
+                s->h_pace[rows] = rec.pace;
+            }
+            rows++;
+        } else {
+            h.log_row = -1;
+        }
+        s->h_tend[n] = rec.t_end;
+        n++;
+    }
+    CK(s, cudaMemcpyAsync(s->d_steps, s->h_steps, n * sizeof(mkg_step),
+                          cudaMemcpyHostToDevice, s->stream));
+
+    /* Launch geometry */
+    const int bx = s->cfg.block_x, by = s->cfg.block_y;
+    const bool two_d = s->cfg.two_d != 0;
+    mkg_launch a;
+    memset(&a, 0, sizeof(a));
+    a.nx = s->cfg.nx;
+    a.ny = s->cfg.ny;
+    a.ncell = s->ncell;
+    a.pitch = s->pitch;
+    a.state = s->d_state;
+    a.vbuf = s->d_vbuf;
+    a.field = s->d_field;
+    a.gx = s->d_gx;
+    a.gy = s->d_gy;
+    a.nbr_ptr = s->d_nbr_ptr;
+    a.nbr_idx = s->d_nbr_idx;
+    a.nbr_g = s->d_nbr_g;
+    a.gxs = s->gx;
+    a.gys = s->gy;
+    a.pace_x0 = s->px0;
+    a.pace_x1 = s->px1;
+    a.pace_y0 = s->py0;
+    a.pace_y1 = s->py1;
+    a.pace_bits = s->d_pace_bits;
+    a.pace_mode = s->pace_mode;
+    a.log = s->d_log;
+    a.log_items = s->d_log_items;
+    a.log_cols = s->d_log_cols;
+    a.log_ncol = s->log_ncol;
+    a.n_log_items = s->n_log_items;
+    a.nan_check = s->nan_check;
+    a.status = s->d_status;
+    a.timeout_ns = s->timeout_ns;
+    if (two_d) {
+        a.ntiles_x = (int)((s->cfg.nx + bx - 1) / bx);
+        a.ntiles_y = (int)((s->cfg.ny + by - 1) / by);
+    } else {
+        /* Flat cell array: 1D cables, connection graphs and diffusion-free
+         * simulations (whose cells are independent). */
+        a.nx = s->ncell;
+        a.ny = 1;
+        a.ntiles_x = (int)((s->ncell + bx - 1) / bx);
+        a.ntiles_y = 1;
+    }
+    const long long ntiles = (long long)a.ntiles_x * a.ntiles_y;
+    int bpsm = s->blocks_per_sm > 0 ? std::min(s->blocks_per_sm, s->occ_blocks)
+                                    : s->occ_blocks;
+    long long coop_blocks = std::min<long long>(ntiles,
+                                                (long long)bpsm * s->num_sms);
+    int spl = s->steps_per_launch > 0 ? s->steps_per_launch : 1 << 20;
+
+    CK(s, cudaEventRecord(s->ev0, s->stream));
+    int64_t done = 0;
+    bool halted = false;
+    mkg_status init;
+    init.barrier = 0;
+    init.error = MKG_DEV_OK;
+    init.halt_step = MKG_NO_HALT;
+    init.timeout_block = -1;
+    while (done < n) {
+        const int64_t m = std::min<int64_t>(n - done, spl);
+        *s->h_status = init;
+        CK(s, cudaMemcpyAsync(s->d_status, s->h_status, sizeof(mkg_status),
+                              cudaMemcpyHostToDevice, s->stream));
+        a.steps = s->d_steps + done;
+        a.nsteps = (int)m;
+        a.v_sel = s->v_sel;
+        void *args[] = {&a};
+        cudaLaunchConfig_t lc;
+        memset(&lc, 0, sizeof(lc));
+        cudaLaunchAttribute attr[1];
+        lc.blockDim = dim3(bx, by, 1);
+        lc.stream = s->stream;
+        if (m > 1) {
+            lc.gridDim = dim3((unsigned)coop_blocks, 1, 1);
+            attr[0].id = cudaLaunchAttributeCooperative;
+            attr[0].val.cooperative = 1;
+            lc.attrs = attr;
+            lc.numAttrs = 1;
+        } else {
+            lc.gridDim = dim3((unsigned)std::min<long long>(ntiles, 1 << 30),
+                              1, 1);
+        }
+        CK(s, cudaLaunchKernelExC(&lc, (const void *)s->kernel, args));
+        s->last_launches++;
+        CK(s, cudaMemcpyAsync(s->h_status, s->d_status, sizeof(mkg_status),
+                              cudaMemcpyDeviceToHost, s->stream));
+        CK(s, cudaStreamSynchronize(s->stream));
+        if (s->h_status->error != MKG_DEV_OK) {
+            s->running = false;
+            return set_err(s, MKG_ERR_TIMEOUT,
+                           "device barrier wait timed out (block %d)",
+                           s->h_status->timeout_block);
+        }
+        int64_t executed = m;
+        if (s->h_status->halt_step != MKG_NO_HALT) {
+            executed = (int64_t)s->h_status->halt_step + 1;
+            halted = true;
+        }
+        s->v_sel ^= (int)(executed & 1);
+        if (!diffusion_on(s)) s->v_sel = 0;
+        done += executed;
+        s->last_cell_steps += executed * s->ncell;
+        if (halted) break;
+    }
+    CK(s, cudaEventRecord(s->ev1, s->stream));
+
+    /* Rows written by the executed steps */
+    int64_t rows_done = 0;
+    for (int64_t i = 0; i < done; ++i)
+        if (s->h_steps[i].log_row >= 0) rows_done = s->h_steps[i].log_row + 1;
+    if (rows_done > 0 && s->log_ncol > 0) {
+        const long long cnt = rows_done * (long long)s->log_ncol;
+        if (s->real == 4)
+            k_log_to_double<float><<<grid_for(cnt), 256, 0, s->stream>>>(
+                (const float *)s->d_log, s->d_log_dbl, cnt);
+        else
+            k_log_to_double<double><<<grid_for(cnt), 256, 0, s->stream>>>(
+                (const double *)s->d_log, s->d_log_dbl, cnt);
+        CK(s, cudaGetLastError());
+        CK(s, cudaMemcpyAsync(s->h_log, s->d_log_dbl, cnt * sizeof(double),
+                              cudaMemcpyDeviceToHost, s->stream));
+    }
+    CK(s, cudaStreamSynchronize(s->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    s->last_ms = ms;
+    s->last_rows = rows_done;
+    if (rows_out) *rows_out = rows_done;
+    const double t = done > 0 ? s->h_tend[done - 1] : s->sched.time();
+    if (t_out) *t_out = t;
+    if (halted) {
+        s->running = false;
+        s->halted = true;
+        return MKG_HALT_NAN;
+    }
+    if (s->sched.done()) {
+        s->running = false;
+        return MKG_DONE;
+    }
+    return MKG_OK;
+}
+
+int mkg_read_log(mkg_sim *s, double *time, double *pace, double *values,
+                 int64_t rows)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (rows < 0 || rows > s->last_rows)
+        return set_err(s, MKG_ERR_ARG, "rows exceeds the rows of the last"
+                       " chunk");
+    if (time) memcpy(time, s->h_time.data(), rows * sizeof(double));
+    if (pace) memcpy(pace, s->h_pace.data(), rows * sizeof(double));
+    if (values && s->log_ncol > 0)
+        memcpy(values, s->h_log, rows * s->log_ncol * sizeof(double));
+    return MKG_OK;
+}
+
+int mkg_last_stats(const mkg_sim *s, double *kernel_ms, int64_t *launches,
+                   int64_t *cell_steps)
+{
+    if (!s) return set_err(nullptr, MKG_ERR_ARG, "null argument");
+    if (kernel_ms) *kernel_ms = s->last_ms;
+    if (launches) *launches = s->last_launches;
+    if (cell_steps) *cell_steps = s->last_cell_steps;
+    return MKG_OK;
+}
+
+int64_t mkg_schedule_preview(const double *events, int64_t n_events,
+                             double tmin, double tmax, double default_dt,
+                             double log_interval, int64_t max_steps,
+                             double *t, double *dt, double *pace,
+                             int32_t *log)
+{
+    mkg::Pacer p;
+    int st = p.populate(events, n_events);
+    if (st != mkg::PACER_OK) return st;
+    mkg::Schedule sc;
+    st = sc.begin(p, tmin, tmax, default_dt, log_interval);
+    if (st != mkg::PACER_OK) return st;
+    int64_t n = 0;
+    while (n < max_steps && !sc.done()) {
+        mkg::StepRecord r;
+        st = sc.next(&r);
+        if (st != mkg::PACER_OK) return st;
+        if (t) t[n] = r.t;
+        if (dt) dt[n] = r.dt;
+        if (pace) pace[n] = r.pace;
+        if (log) log[n] = r.log ? 1 : 0;
+        n++;
+    }
+    return n;
+}
+
+}  /* extern "C" */

@@ -1,0 +1,67 @@
+/*
+ * mkg_kernel_abi.h -- argument block shared by the host library and the
+ * generated tissue kernels. Included by mkg_host.cu and prepended (as text)
+ * to every generated kernel compiled with NVRTC, so both sides agree on the
+ * layout. Plain C types only: NVRTC compiles it without system headers.
+ */
+#ifndef MKG_KERNEL_ABI_H
+#define MKG_KERNEL_ABI_H
+
+/* Device error codes written to mkg_status.error */
+#define MKG_DEV_OK        0
+#define MKG_DEV_TIMEOUT   1   /* grid barrier wait exceeded timeout_ns */
+
+#define MKG_NO_HALT 0x7fffffff
+
+/* One time step of the schedule, computed on the host exactly as the
+ * reference's sim_step loop does (openclsim.c:1051-1063). The kernel casts
+ * t, dt and pace to its Real type, as the reference casts its kernel
+ * arguments (openclsim.c:1063, 1148, 1155). */
+typedef struct mkg_step {
+    double t;          /* engine time at the start of the step */
+    double dt;         /* step size */
+    double pace;       /* global pacing level during the step */
+    int log_row;       /* row of the chunk log written at this step, or -1 */
+    int pad;
+} mkg_step;
+
+/* Device-side status word, one per simulation. */
+typedef struct mkg_status {
+    unsigned int barrier;   /* grid barrier arrival counter (reset per launch) */
+    int error;              /* MKG_DEV_* */
+    int halt_step;          /* first step of the launch that saw the NaN halt */
+    int timeout_block;      /* block that gave up waiting, for diagnostics */
+} mkg_status;
+
+/* Everything a tissue step launch needs. Passed by value. */
+typedef struct mkg_launch {
+    long long nx, ny;        /* grid shape */
+    long long ncell;         /* nx * ny */
+    long long pitch;         /* cells per plane in the SoA buffers */
+    void *state;             /* Real[n_state][pitch] */
+    void *vbuf;              /* Real[2][pitch]: V(t) and V(t+dt) ping-pong */
+    const void *field;       /* Real[n_field][pitch] */
+    const void *gx;          /* heterogeneous x conductances, ny*(nx-1) */
+    const void *gy;          /* heterogeneous y conductances, (ny-1)*nx */
+    const int *nbr_ptr;      /* CSR row pointers, ncell + 1 */
+    const int *nbr_idx;      /* CSR neighbour cell ids */
+    const void *nbr_g;       /* CSR conductances (Real) */
+    double gxs, gys;         /* homogeneous conductances */
+    long long pace_x0, pace_x1, pace_y0, pace_y1;  /* paced rectangle */
+    const unsigned int *pace_bits;                 /* paced list bitmap */
+    const mkg_step *steps;   /* nsteps schedule entries */
+    void *log;               /* Real[rows][log_ncol] */
+    const int *log_items;    /* item id of each logged item slot */
+    const int *log_cols;     /* int[n_log_items][pitch]: column or -1 */
+    mkg_status *status;
+    long long timeout_ns;    /* bound on each grid barrier wait */
+    int pace_mode;           /* MKG_PACE_* */
+    int nsteps;              /* steps in this launch */
+    int v_sel;               /* plane of vbuf holding V(t) at step 0 */
+    int log_ncol;
+    int n_log_items;
+    int nan_check;           /* apply the NaN halt at log rows */
+    int ntiles_x, ntiles_y;  /* tiles covering the grid (2D) or cells (1D) */
+} mkg_launch;
+
+#endif /* MKG_KERNEL_ABI_H */

@@ -1,0 +1,523 @@
+"""
+CUDA exporter: turns a myokit model into one fused tissue-step kernel.
+
+The reference renders ``myokit/_sim/openclsim.cl`` once per run into an
+OpenCL program with a ``cell_step`` kernel (model right-hand side plus the
+forward-Euler or Rush-Larsen update, ``openclsim.cl:298-367``) and separate
+diffusion kernels (``diff_step`` ``:384``, ``diff_hetero`` ``:452``,
+``diff_arb_step`` ``:537``). This exporter emits a single CUDA kernel,
+``mkg_tissue_step``, that for every cell and step
+
+1. computes the diffusion current from V(t) of the neighbours (shared-memory
+   halo tile for 2D grids, neighbour list for arbitrary connections),
+2. evaluates the model right-hand side in registers,
+3. writes the logged values of that step to the device log, and
+4. updates every state to t + dt, writing V(t + dt) to the second plane of a
+   ping-pong buffer so that neighbours still read V(t).
+
+Several steps run in one launch, separated by a bounded grid barrier. State
+is stored structure-of-arrays, so every load and store is coalesced.
+
+Differences from the reference kernel text that do not change results:
+
+- constants that do not depend on a scalar field are evaluated once on the
+  host (in the simulation precision, with ``Expression.eval``) and written as
+  literals, where the reference writes them as macros (``openclsim.cl:174-186``);
+- small integer powers ``x^2``, ``x^3``, ``x^4`` are written as products.
+"""
+import hashlib
+import os
+
+import numpy as np
+
+from ._deps import myokit
+from myokit.formats.ansic import CBasedExpressionWriter
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_CSRC = os.path.join(_HERE, 'csrc')
+
+# Diffusion modes (match include/mkg_tissue.h)
+DIFF_NONE = 0
+DIFF_GRID = 1
+DIFF_HETERO = 2
+DIFF_CONN = 3
+
+# Bound-variable internal names used in the generated code
+_T = 't_'
+_PACE = 'pace_'
+_IDIFF = 'idiff_'
+
+
+def _fmt_number(x, single):
+    """Formats a float as a C literal of the simulation precision."""
+    x = float(x)
+    if np.isnan(x):
+        return '(0.0f/0.0f)' if single else '(0.0/0.0)'
+    if np.isinf(x):
+        s = '(1.0f/0.0f)' if single else '(1.0/0.0)'
+        return s if x > 0 else '(-' + s + ')'
+    # Shortest text that rounds back to the same value in the precision
+    s = str(np.float32(x)) if single else repr(x)
+    if 'e' not in s and '.' not in s:
+        s += '.0'
+    return s + 'f' if single else s
+
+
+class CudaExpressionWriter(CBasedExpressionWriter):
+    """
+    Writes myokit expressions as CUDA C++ for one precision.
+
+    Functions are written with explicit single or double precision names
+    (``expf``/``exp``); with ``native_math`` the single precision versions
+    use the fast hardware approximations (``__expf`` etc.), the CUDA
+    counterpart of OpenCL's ``native_*`` functions
+    (``myokit/formats/opencl/_ewriter.py:59-93``).
+    """
+    def __init__(self, single, native_math=False):
+        super().__init__()
+        self._single = bool(single)
+        self._native = bool(native_math) and self._single
+
+    def _fn(self, name):
+        if not self._single:
+            return name
+        if self._native and name in ('exp', 'log', 'sin', 'cos', 'tan',
+                                     'log10'):
+            return '__' + name + 'f'
+        return name + 'f'
+
+    def _ex_number(self, e):
+        return _fmt_number(e.eval(), self._single)
+
+    def _ex_power(self, e):
+        base, exponent = e[0], e[1]
+        if isinstance(exponent, myokit.Number):
+            p = exponent.eval()
+            if p in (2.0, 3.0, 4.0):
+                return f'mkg_pow{int(p)}({self.ex(base)})'
+        return f'{self._fn("pow")}({self.ex(base)}, {self.ex(exponent)})'
+
+    def _ex_sqrt(self, e):
+        return self._ex_function(e, self._fn('sqrt'))
+
+    def _ex_sin(self, e):
+        return self._ex_function(e, self._fn('sin'))
+
+    def _ex_cos(self, e):
+        return self._ex_function(e, self._fn('cos'))
+
+    def _ex_tan(self, e):
+        return self._ex_function(e, self._fn('tan'))
+
+    def _ex_asin(self, e):
+        return self._ex_function(e, self._fn('asin'))
+
+    def _ex_acos(self, e):
+        return self._ex_function(e, self._fn('acos'))
+
+    def _ex_atan(self, e):
+        return self._ex_function(e, self._fn('atan'))
+
+    def _ex_exp(self, e):
+        return self._ex_function(e, self._fn('exp'))
+
+    def _ex_log(self, e):
+        f = self._fn('log')
+        if len(e) == 1:
+            return self._ex_function(e, f)
+        return f'({f}({self.ex(e[0])}) / {f}({self.ex(e[1])}))'
+
+    def _ex_log10(self, e):
+        return self._ex_function(e, self._fn('log10'))
+
+    def _ex_floor(self, e):
+        return self._ex_function(e, self._fn('floor'))
+
+    def _ex_ceil(self, e):
+        return self._ex_function(e, self._fn('ceil'))
+
+    def _ex_abs(self, e):
+        return self._ex_function(e, self._fn('fabs'))
+
+
+class OpCensus(object):
+    """
+    Counts the work in one cell-step of a generated kernel: arithmetic
+    operations (``+ - * /``, an FMA counted as two), transcendental calls and
+    conditionals. Used for the compute roofline.
+    """
+    _TRANS = (
+        myokit.Exp, myokit.Log, myokit.Log10, myokit.Sqrt, myokit.Sin,
+        myokit.Cos, myokit.Tan, myokit.ASin, myokit.ACos, myokit.ATan)
+
+    def __init__(self):
+        self.arith = 0
+        self.divide = 0
+        self.trans = 0
+        self.power = 0
+        self.cond = 0
+
+    def add(self, e):
+        for x in e.walk():
+            if isinstance(x, (myokit.Plus, myokit.Minus, myokit.Multiply,
+                              myokit.PrefixMinus)):
+                self.arith += 1
+            elif isinstance(x, (myokit.Divide, myokit.Quotient,
+                                myokit.Remainder)):
+                self.arith += 1
+                self.divide += 1
+            elif isinstance(x, myokit.Power):
+                p = x[1].eval() if isinstance(x[1], myokit.Number) else None
+                if p in (2.0, 3.0, 4.0):
+                    self.arith += int(p) - 1
+                else:
+                    self.power += 1
+            elif isinstance(x, self._TRANS):
+                self.trans += 1
+            elif isinstance(x, (myokit.If, myokit.Piecewise)):
+                self.cond += 1
+
+    def as_dict(self):
+        return {
+            'arith': self.arith, 'divide': self.divide, 'trans': self.trans,
+            'power': self.power, 'cond': self.cond,
+        }
+
+
+# Writes the logged items of one class for this cell at a log row.
+_LOG_BLOCK = '''
+        if (row >= 0) {{
+            Real *lg = (Real *)a.log + (long long)row * a.log_ncol;
+            for (int j = 0; j < a.n_log_items; ++j) {{
+                const int item = a.log_items[j];
+                if (!({cond})) continue;
+                const int c = a.log_cols[(long long)j * pitch + cid];
+                if (c < 0) continue;
+                Real val = 0;
+                switch (item) {{
+                {cases}
+                default: break;
+                }}
+                lg[c] = val;
+            }}
+        }}'''
+
+
+def _read(name):
+    with open(os.path.join(_CSRC, name), 'r') as f:
+        return f.read()
+
+
+class TissueKernel(object):
+    """
+    The generated CUDA source for one simulation configuration, with the
+    metadata the host needs (state order, logged intermediaries, census).
+
+    Arguments:
+
+    ``model``
+        A cloned model with unique names created and bindings prepared, as
+        held by :class:`SimulationCUDA` (``openclsim.py:276-290``).
+    ``precision``
+        ``myokit.SINGLE_PRECISION`` or ``myokit.DOUBLE_PRECISION``.
+    ``native_math``
+        Use fast hardware approximations for single precision functions.
+    ``bound_variables``
+        Map from bound variables to ``'time'``, ``'pace'`` or ``'idiff'``.
+    ``inter_log``
+        Intermediary variables whose values are logged.
+    ``diffusion``
+        One of ``DIFF_NONE``, ``DIFF_GRID``, ``DIFF_HETERO``, ``DIFF_CONN``.
+    ``two_d``
+        True for an ``(nx, ny)`` grid.
+    ``fields``
+        Variables replaced by per-cell scalar fields, in field order.
+    ``rl_states``
+        Map ``{state: (inf, tau)}`` of Rush-Larsen states.
+    ``block``
+        CTA shape ``(bx, by)``.
+    ``fast_divide``
+        Single precision only: use the 2-ulp division of the hardware,
+        within the 2.5 ulp that OpenCL allows for ``x / y`` by default.
+    """
+    def __init__(self, model, precision, native_math, bound_variables,
+                 inter_log, diffusion, two_d, fields, rl_states, block,
+                 fast_divide=True, min_blocks=1):
+        self.model = model
+        self.single = (precision == myokit.SINGLE_PRECISION)
+        self.native_math = bool(native_math)
+        self.bound = dict(bound_variables)
+        self.inter_log = list(inter_log)
+        self.diffusion = int(diffusion)
+        self.two_d = bool(two_d) and self.diffusion in (DIFF_GRID, DIFF_HETERO)
+        self.fields = list(fields)
+        self.rl_states = dict(rl_states)
+        self.block = (int(block[0]), int(block[1]))
+        self.fast_divide = bool(fast_divide) and self.single
+        self.min_blocks = int(min_blocks)
+        self.states = list(model.states())
+        self.n_state = len(self.states)
+        self.vm = model.label('membrane_potential')
+        if self.diffusion != DIFF_NONE:
+            self.i_vm = self.vm.index()
+        else:
+            self.i_vm = -1
+        self.census = OpCensus()
+        self._source = self._generate()
+
+    # -- naming ------------------------------------------------------------
+
+    def _name(self, x):
+        """C name of a variable or LhsExpression."""
+        if isinstance(x, myokit.Derivative):
+            return 'd_' + x.var().uname()
+        if isinstance(x, myokit.Name):
+            x = x.var()
+        b = self.bound.get(x)
+        if b == 'time':
+            return _T
+        if b == 'pace':
+            return _PACE
+        if b == 'idiff':
+            return _IDIFF
+        if x.is_state():
+            return 'x_' + x.uname()
+        return 'v_' + x.uname()
+
+    # -- generation --------------------------------------------------------
+
+    def _generate(self):
+        m = self.model
+        w = CudaExpressionWriter(self.single, self.native_math)
+        w.set_lhs_function(self._name)
+        real = 'float' if self.single else 'double'
+        prec = myokit.SINGLE_PRECISION if self.single else \
+            myokit.DOUBLE_PRECISION
+
+        order = m.solvable_order()
+        remaining = order.pop('*remaining*', None)
+        if remaining is not None and len(remaining) > 0:
+            raise ValueError(
+                'This simulation requires models without interdependent'
+                ' components.')
+
+        field_set = set(self.fields)
+
+        # Constants that depend (directly or not) on a field must be computed
+        # per cell; all others are folded to literals on the host.
+        percell_const = set()
+        const_eqs = []
+        for group in order.values():
+            for eq in group.equations(const=True):
+                const_eqs.append(eq)
+        changed = True
+        while changed:
+            changed = False
+            for eq in const_eqs:
+                var = eq.lhs.var()
+                if var in percell_const:
+                    continue
+                if var in field_set:
+                    percell_const.add(var)
+                    changed = True
+                    continue
+                for ref in eq.rhs.references():
+                    if ref.var() in percell_const:
+                        percell_const.add(var)
+                        changed = True
+                        break
+
+        # Host-folded constant values (in the simulation precision)
+        literal_subst = {}
+        for eq in const_eqs:
+            var = eq.lhs.var()
+            if var in percell_const or var in self.bound:
+                continue
+            value = eq.rhs.eval(precision=prec)
+            literal_subst[myokit.Name(var)] = myokit.Number(float(value))
+
+        def fold(e):
+            if literal_subst:
+                return e.clone(subst=literal_subst)
+            return e
+
+        body = []
+        tab = '        '
+
+        # Per-cell constants (fields and what depends on them), in order
+        body.append(tab + '// Per-cell constants (scalar fields)')
+        for k, var in enumerate(self.fields):
+            body.append(
+                f'{tab}const Real {self._name(var)} = '
+                f'field[(long long){k} * pitch + cid];')
+        for eq in const_eqs:
+            var = eq.lhs.var()
+            if var in percell_const and var not in field_set:
+                rhs = fold(eq.rhs)
+                self.census.add(rhs)
+                body.append(
+                    f'{tab}const Real {self._name(var)} = {w.ex(rhs)};')
+
+        def ref(var):
+            # Name of a variable, or its literal when it was folded
+            x = literal_subst.get(myokit.Name(var))
+            return w.ex(x) if x is not None else self._name(var)
+
+        # State loads, and the update of each state, emitted as soon as its
+        # inputs exist so that derivatives do not stay live to the end.
+        loads = []
+        updates = []
+        for i, s in enumerate(self.states):
+            n = self._name(s)
+            if i == self.i_vm:
+                loads.append(f'{tab}const Real {n} = V_;')
+            else:
+                loads.append(
+                    f'{tab}const Real {n} = state[(long long){i} * pitch'
+                    f' + cid];')
+            if s in self.rl_states:
+                inf, tau = self.rl_states[s]
+                need = set(
+                    self._name(v) for v in (inf, tau)
+                    if myokit.Name(v) not in literal_subst)
+                inf, tau = ref(inf), ref(tau)
+                expf = w._fn('exp')
+                upd = f'{inf} - ({inf} - {n}) * {expf}(-dt_ / {tau})'
+                self.census.arith += 4
+                self.census.trans += 1
+            else:
+                need = set([self._name(s.lhs())])
+                upd = f'{n} + dt_ * {self._name(s.lhs())}'
+                self.census.arith += 2
+            if i == self.i_vm:
+                text = f'{tab}vout[cid] = {upd};'
+            else:
+                text = f'{tab}state[(long long){i} * pitch + cid] = {upd};'
+            updates.append((i, need, text))
+
+        defined = set(self._name(v) for v in self.fields)
+        for eq in const_eqs:
+            if eq.lhs.var() in percell_const:
+                defined.add(self._name(eq.lhs.var()))
+        emitted = set()
+
+        def flush():
+            for i, need, text in updates:
+                if i not in emitted and need <= defined:
+                    body.append(text)
+                    emitted.add(i)
+
+        # Equations in solvable order (the reference calls one function per
+        # component in this order, openclsim.cl:336-352).
+        body.append(tab + '// Model right-hand side at time t')
+        flush()
+        for group in order.values():
+            for eq in group.equations(const=False):
+                var = eq.lhs.var()
+                if var in self.bound:
+                    continue
+                if isinstance(eq.lhs, myokit.Derivative) and \
+                        var in self.rl_states:
+                    continue
+                rhs = fold(eq.rhs)
+                self.census.add(rhs)
+                name = self._name(eq.lhs)
+                body.append(f'{tab}const Real {name} = {w.ex(rhs)};')
+                defined.add(name)
+                flush()
+        if len(emitted) != len(updates):   # pragma: no cover
+            raise ValueError('Could not order the state updates.')
+        self._inter_names = [self._name(v) for v in self.inter_log]
+
+        # Logging: states and idiff right after the loads, intermediaries
+        # at the end (item ids as in include/mkg_tissue.h).
+        t2 = tab + '    '
+        cases = [f'case {i}: val = {self._name(s)}; break;'
+                 for i, s in enumerate(self.states)]
+        cases.append(f'case {self.n_state}: val = {_IDIFF}; break;')
+        log_a = _LOG_BLOCK.format(
+            cond=f'item <= {self.n_state}',
+            cases=('\n' + t2 + '        ').join(cases))
+        first = self._name(self.states[0])
+        log_a += (
+            f'\n{tab}if (row >= 0 && a.nan_check && cid == 0 && '
+            f'isnan({first}))\n{tab}    atomicMin(&a.status->halt_step, k);')
+        log_b = ''
+        if self.inter_log:
+            cases = [f'case {self.n_state + 1 + k}: val = {name}; break;'
+                     for k, name in enumerate(self._inter_names)]
+            log_b = _LOG_BLOCK.format(
+                cond=f'item > {self.n_state}',
+                cases=('\n' + t2 + '        ').join(cases))
+
+        subs = {
+            '@REAL@': real,
+            '@SINGLE@': '1' if self.single else '0',
+            '@N_STATE@': str(self.n_state),
+            '@N_FIELD@': str(len(self.fields)),
+            '@N_INTER@': str(len(self.inter_log)),
+            '@I_VM@': str(self.i_vm),
+            '@DIFF@': str(self.diffusion),
+            '@TWO_D@': '1' if self.two_d else '0',
+            '@BX@': str(self.block[0]),
+            '@BY@': str(self.block[1]),
+            '@MINB@': str(self.min_blocks),
+            '@LOADS@': '\n'.join(loads),
+            '@LOG_A@': log_a,
+            '@BODY@': '\n'.join(body),
+            '@LOG_B@': log_b,
+        }
+        text = _read('tissue_kernel.cu.in')
+        for k, v in subs.items():
+            text = text.replace(k, v)
+        abi = _read('mkg_kernel_abi.h')
+        return (
+            '// Generated by myokit_gb300.exporter for model '
+            + str(m.name()) + '\n' + abi + '\n' + text)
+
+    # -- public ------------------------------------------------------------
+
+    def source(self):
+        """Returns the CUDA C++ source text."""
+        return self._source
+
+    def options(self):
+        """NVRTC options for this kernel."""
+        opts = [
+            '--gpu-architecture=sm_103a',
+            '--std=c++17',
+            '-lineinfo',
+            '--extra-device-vectorization',
+        ]
+        if self.single:
+            if self.fast_divide:
+                opts.append('--prec-div=false')
+            opts.append('--prec-sqrt=false' if self.native_math else
+                        '--prec-sqrt=true')
+            opts.append('--ftz=false')
+        opts.append('--fmad=true')
+        return opts
+
+    def key(self):
+        """A hash identifying the source and options, for the cubin cache."""
+        h = hashlib.sha256()
+        h.update(self._source.encode())
+        h.update('\0'.join(self.options()).encode())
+        return h.hexdigest()
+
+    def bytes_per_cell_step(self):
+        """
+        Algorithmic bytes per cell-step: one read and one write of every
+        state, one read of every field and, for heterogeneous grids, of two
+        conductances. Neighbour V reads count as on-chip hits.
+        """
+        r = 4 if self.single else 8
+        b = 2 * self.n_state * r + len(self.fields) * r
+        if self.diffusion == DIFF_HETERO:
+            b += 2 * r
+        return b
+
+    def flops_per_cell_step(self):
+        """Arithmetic operations per cell-step (excluding transcendentals),
+        plus about 8 for the diffusion current."""
+        return self.census.arith + (8 if self.diffusion else 0)
