@@ -1,0 +1,418 @@
+#!/usr/bin/env python3
+"""
+Headline benchmark: cell-steps/s of the fused tissue step on one GB300.
+
+Workload (a 2D sheet as in the reference's SimulationOpenCL use):
+  512 x 512 cells, Rush-Larsen on, dt = 0.005 ms, the 4 left columns paced
+  by a 1 Hz protocol (2 ms pulses, level 1), per-cell GKr and GNa scale
+  fields lognormal(0, 0.2) from a seed, V logged every 1 ms at 256 seeded
+  random probe cells. The O'Hara-Rudy 2011 model file is not available, so
+  the 48-state Decker 2009 canine model shipped with myokit stands in.
+
+One bench step = ``run(step_ms)`` of that sheet (2000 time steps at the
+default 10 ms). ``value`` is cell-steps per second of device time with the
+state resident in HBM (CUDA events on the simulation's stream around the
+kernel launches); ``e2e`` is the same metric through the public
+``SimulationCUDA.run`` call, state upload, log and final state download
+included. Single precision is the headline; double precision is timed on
+the same sheet and the largest |dV| between the two at the probes is
+reported.
+
+--impl reference times the reference's own kernel (the OpenCL C that
+myokit's SimulationOpenCL renders for this model, compiled for the host
+CPU and driven by the oracle's restatement of the reference step loop) on
+all host cores, with the same metric and configuration.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'cell-steps/s on 1 GB300 (FP32 vs FP64 at stated max|dV|)'
+UNIT = 'cell-steps/s'
+
+
+def parse():
+    p = argparse.ArgumentParser(description=__doc__.split('\n')[1])
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=10)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    p.add_argument('--size', type=int, default=512)
+    p.add_argument('--step-ms', type=float, default=10.0)
+    p.add_argument('--fp64-steps', type=int, default=2,
+                   help='timed double precision bench steps (0 = skip)')
+    p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--cpu-seconds', type=float, default=12.0,
+                   help='target CPU work for the cpu_baseline sample')
+    return p.parse_args()
+
+
+def load_model():
+    from myokit_gb300._deps import myokit
+    path = os.path.join(os.path.dirname(myokit.__file__), 'tests', 'data',
+                        'decker-2009.mmt')
+    return myokit.load_model(path)
+
+
+def make_sheet(cls, precision, size, seed=0, **kw):
+    """The benchmark sheet; returns (simulation, log variable list)."""
+    from myokit_gb300._deps import myokit
+    m = load_model()
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    s = cls(m, p, ncells=(size, size), precision=precision, rl=True, **kw)
+    s.set_step_size(0.005)
+    s.set_paced_cells(nx=4, ny=size, x=0, y=0)
+    rng = np.random.default_rng(seed)
+    gkr = m.get('ikr.Gbar').eval()
+    gna = m.get('ina.Gbar').eval()
+    s.set_field('ikr.Gbar', gkr * rng.lognormal(0, 0.2, (size, size)))
+    s.set_field('ina.Gbar', gna * rng.lognormal(0, 0.2, (size, size)))
+    cells = rng.choice(size * size, 256, replace=False)
+    log = ['engine.time'] + [
+        '%d.%d.membrane.V' % (c % size, c // size) for c in sorted(cells)]
+    return s, log
+
+
+def config(args, workload):
+    return {
+        'workload': workload,
+        'model': 'decker-2009 (48 states; stands in for O\'Hara-Rudy 2011'
+                 ' endo, whose model file is unavailable)',
+        'grid': [args.size, args.size],
+        'rl': True, 'dt_ms': 0.005, 'step_ms': args.step_ms,
+        'paced': 'left 4 columns, 1 Hz, 2 ms, level 1',
+        'fields': 'GKr, GNa x lognormal(0, 0.2), seed 0',
+        'log': 'V at 256 probes every 1 ms',
+        'l2': 'flushed between timed steps (256 MiB write)',
+    }
+
+
+class ClockSampler(object):
+    """Samples nvidia-smi clocks and throttle reasons in the background."""
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,'
+              'clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, out=None):
+        self.proc = None
+        self.out = out
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '--query-gpu=' + self.FIELDS,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        self.lines = []
+        if self.proc is not None:
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:   # pragma: no cover
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown',
+                 'sw_power_cap']
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(name)
+        if self.out:
+            with open(self.out, 'w') as f:
+                f.write('\n'.join(self.lines) + '\n')
+        if not sm:
+            return None
+        return {'sm_mhz': float(np.median(sm)), 'sm_max_mhz': max(mx),
+                'samples': len(sm), 'reasons': sorted(reasons)}
+
+
+def read_peaks():
+    path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 'fallback'
+
+
+def read_traffic():
+    """Per-cell-step DRAM bytes of the tissue kernel from the committed ncu
+    summary, or None."""
+    path = os.path.join(ROOT, 'profiles', 'tissue_step_traffic.json')
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(args, precision, seconds):
+    """Times the reference kernel on the host cores for a bounded sample."""
+    from oracle.refsim import ReferenceCpuSimulation
+    cores = os.cpu_count() or 1
+    s, _ = make_sheet(ReferenceCpuSimulation, precision, args.size)
+    s.set_threads(cores)
+    ncell = args.size * args.size
+    # Calibrate on a short run, then size the sample
+    t0 = time.perf_counter()
+    s.run(0.05, log=['engine.time'], log_interval=1)   # 10 steps
+    dt = time.perf_counter() - t0
+    rate0 = ncell * 10 / max(dt, 1e-9)
+    nsteps = int(max(20, min(20000, rate0 * seconds / ncell)))
+    t0 = time.perf_counter()
+    s.run(nsteps * 0.005, log=['engine.time'], log_interval=1)
+    dt = time.perf_counter() - t0
+    return {
+        'value': ncell * nsteps / dt, 'unit': UNIT, 'cores': cores,
+        'kind': 'reference',
+        'sample': '%d time steps (%.3g ms) of the %dx%d sheet, %s; the'
+                  ' reference-rendered OpenCL kernel compiled as C (gcc -O2,'
+                  ' OpenMP) with the oracle host loop' % (
+                      nsteps, nsteps * 0.005, args.size, args.size,
+                      'single precision' if precision == 32 else
+                      'double precision'),
+        'seconds': dt,
+    }
+
+
+def run_reference(args):
+    """--impl reference: the reference kernel on the host cores."""
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return 0
+    from myokit_gb300._deps import myokit
+    from oracle.refsim import ReferenceCpuSimulation
+    cores = os.cpu_count() or 1
+    s, log = make_sheet(ReferenceCpuSimulation, myokit.SINGLE_PRECISION,
+                        args.size)
+    s.set_threads(cores)
+    ncell = args.size * args.size
+    # Bench step: a bounded sample sized to ~2 s of CPU time
+    t0 = time.perf_counter()
+    s.run(0.05, log=log, log_interval=1)
+    rate0 = ncell * 10 / max(time.perf_counter() - t0, 1e-9)
+    nsteps = int(max(10, min(2000, rate0 * 2.0 / ncell)))
+    dur = nsteps * 0.005
+    for _ in range(args.warmup):
+        s.run(dur, log=log, log_interval=1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.run(dur, log=log, log_interval=1)
+    dt = time.perf_counter() - t0
+    value = ncell * nsteps * args.steps / dt
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT,
+        'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': dt * 1000 / args.steps, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'data': 'synthetic (seeded fields and probes)',
+        'config': config(args, 'reference kernel on host CPU, %d time steps'
+                         ' per step' % nsteps),
+        'cpu_baseline': {
+            'value': value, 'unit': UNIT, 'cores': cores,
+            'kind': 'reference',
+            'sample': '%d time steps of the %dx%d sheet per step' % (
+                nsteps, args.size, args.size)},
+        'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+
+    def barrier():
+        if dist is not None:
+            dist.barrier(device_ids=[local])
+        torch.cuda.synchronize()
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device='cuda')
+    ncell = args.size * args.size
+    nsteps_per = int(round(args.step_ms / 0.005))
+
+    # --- single precision (headline) -------------------------------------
+    s, log = make_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION,
+                        args.size, seed=rank, device=local)
+    logs32 = []
+    for _ in range(args.warmup):
+        logs32.append(s.run(args.step_ms, log=log, log_interval=1))
+    kernel = s._last_kernel
+    sampler = ClockSampler(os.path.join(ROOT, 'gpurun_out', 'clocks.csv')
+                           if os.path.isdir(os.path.join(ROOT, 'gpurun_out'))
+                           else None)
+    sampler.start()
+    barrier()
+    dev_ms = 0.0
+    wall = 0.0
+    launches = 0
+    step_launches = 0
+    cell_steps = 0
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        logs32.append(s.run(args.step_ms, log=log, log_interval=1))
+        wall += time.perf_counter() - t0
+        st = s.last_run_stats()
+        dev_ms += st['kernel_ms']
+        launches += st['all_launches']
+        step_launches += st['launches']
+        cell_steps += st['cell_steps']
+    barrier()
+    clocks = sampler.stop()
+    if dist is not None:
+        t = torch.tensor([dev_ms, wall], dtype=torch.float64, device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms, wall = float(t[0]), float(t[1])
+    total_cell_steps = cell_steps * world
+    value = total_cell_steps / (dev_ms / 1000.0)
+    e2e_value = total_cell_steps / wall
+
+    # Bytes crossing the host boundary per bench step (public run() call)
+    nstate = s._nstate
+    h2d = ncell * nstate * 8 + ncell * 2 * 8 + nsteps_per * 32
+    d2h = ncell * nstate * 8 + (len(log) - 1) * int(args.step_ms) * 8
+
+    # Roofline of the tissue kernel (algorithmic bytes per launch)
+    bpcs = kernel.bytes_per_cell_step()
+    avg_launch_s = (dev_ms / 1000.0) / max(step_launches, 1)
+    per_launch_cs = cell_steps / max(step_launches, 1)
+    achieved = bpcs * per_launch_cs / avg_launch_s / 1e9
+    peak, peak_kind = read_peaks()
+    traffic = read_traffic()
+    traffic_per_launch = None
+    if traffic and traffic.get('bytes_per_cell_step'):
+        traffic_per_launch = traffic['bytes_per_cell_step'] * per_launch_cs
+    # Compute roofline: FP32 lanes x 2 flops x SM clock under load
+    sm_mhz = clocks['sm_mhz'] if clocks else 1900.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    flops = kernel.flops_per_cell_step() * value / world / 1e12
+
+    # --- double precision, same sheet --------------------------------------
+    fp64 = None
+    dv = None
+    if args.fp64_steps > 0 and rank == 0:
+        s64, _ = make_sheet(mg.SimulationCUDA, myokit.DOUBLE_PRECISION,
+                            args.size, seed=rank, device=local)
+        logs64 = []
+        d64 = 0.0
+        n64 = 0
+        nrun = args.warmup + args.fp64_steps
+        for i in range(nrun):
+            logs64.append(s64.run(args.step_ms, log=log, log_interval=1))
+            if i >= args.warmup:
+                st = s64.last_run_stats()
+                d64 += st['kernel_ms']
+                n64 += st['cell_steps']
+        fp64 = {'value': n64 / (d64 / 1000.0), 'unit': UNIT,
+                'steps': args.fp64_steps, 'warmup': args.warmup}
+        worst = 0.0
+        for a, b in zip(logs32[:nrun], logs64):
+            for k in a.keys():
+                if k == 'engine.time':
+                    continue
+                worst = max(worst, float(np.max(np.abs(
+                    np.asarray(a[k], dtype=float) -
+                    np.asarray(b[k], dtype=float)))))
+        dv = {'max_abs_dV_mV': worst,
+              'window_ms': nrun * args.step_ms,
+              'against': 'this sheet in double precision on the GPU'}
+        fp64['speedup_fp32_over_fp64'] = value / world / fp64['value']
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        cpu = cpu_baseline(args, myokit.SINGLE_PRECISION, args.cpu_seconds)
+
+    if rank != 0:
+        return 0
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
+        'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': dev_ms / args.steps, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'data': 'synthetic (seeded fields and probes)',
+        'config': config(args, 'sheet %dx%d, %d time steps per step' % (
+            args.size, args.size, nsteps_per)),
+        'e2e': {'value': e2e_value, 'unit': UNIT, 'h2d_bytes_per_step': h2d,
+                'd2h_bytes_per_step': d2h},
+        'gpu_launches': launches,
+        'roofline': {
+            'bound': 'hbm', 'achieved': achieved, 'peak': peak,
+            'unit': 'GB/s', 'frac': achieved / peak,
+            'traffic': traffic_per_launch,
+            'peak_source': peak_kind,
+            'bytes_per_cell_step': bpcs,
+            'compute': {
+                'unit': 'TFLOP/s', 'achieved': flops, 'peak': fp32_peak,
+                'frac': flops / fp32_peak,
+                'flops_per_cell_step': kernel.flops_per_cell_step(),
+                'transcendentals_per_cell_step': kernel.census.trans,
+                'peak_source': 'FP32 lanes x 2 x median SM clock'},
+        },
+        'fp64': fp64,
+        'accuracy': dv,
+        'clocks': clocks,
+        'cpu_baseline': cpu,
+    }
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

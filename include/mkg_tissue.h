@@ -181,6 +181,14 @@ int mkg_set_tuning(mkg_sim *sim, int32_t steps_per_launch,
 int mkg_last_stats(const mkg_sim *sim, double *kernel_ms, int64_t *launches,
                    int64_t *cell_steps);
 
+/* The cudaStream_t (as void*) all work of this handle is queued on, so a
+ * caller can time it with events recorded on the same stream. */
+int mkg_stream(const mkg_sim *sim, void **stream);
+
+/* Kernels this handle has launched since it was created (tissue steps,
+ * layout and precision conversions). */
+int mkg_launch_count(const mkg_sim *sim, int64_t *count);
+
 /*
  * Host-only view of the step schedule that mkg_run_chunk follows: the first
  * at most max_steps steps of a run over [tmin, tmax) with the given protocol

@@ -101,6 +101,9 @@ SIGNATURES = {
         ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     'mkg_last_stats': (ctypes.c_int, [
         ctypes.c_void_p, _c_double_p, _c_int64_p, _c_int64_p]),
+    'mkg_launch_count': (ctypes.c_int, [ctypes.c_void_p, _c_int64_p]),
+    'mkg_stream': (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     'mkg_schedule_preview': (ctypes.c_int64, [
         _c_double_p, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
         ctypes.c_double, ctypes.c_double, ctypes.c_int64, _c_double_p,

@@ -163,6 +163,7 @@ struct mkg_sim {
 
     double last_ms = 0;
     int64_t last_launches = 0, last_cell_steps = 0;
+    int64_t n_launches = 0;   /* every kernel launched by this handle */
 };
 
 namespace {
@@ -243,6 +244,7 @@ int upload_soa(mkg_sim *s, const double *aos, int nvar, void *dst,
     if (r) return r;
     CK(s, cudaMemcpyAsync(s->d_stage, aos, bytes, cudaMemcpyHostToDevice,
                           s->stream));
+    s->n_launches++;
     k_aos_to_soa<Real><<<grid_for(s->ncell * nvar), 256, 0, s->stream>>>(
         s->d_stage, (Real *)dst, s->ncell, nvar, s->pitch, skip_var,
         (Real *)alt);
@@ -258,6 +260,7 @@ int download_soa(mkg_sim *s, double *aos, int nvar, const void *src,
     const size_t bytes = (size_t)s->ncell * nvar * sizeof(double);
     int r = ensure_stage(s, bytes);
     if (r) return r;
+    s->n_launches++;
     k_soa_to_aos<Real><<<grid_for(s->ncell * nvar), 256, 0, s->stream>>>(
         (const Real *)src, s->d_stage, s->ncell, nvar, s->pitch, skip_var,
         (const Real *)alt);
@@ -276,6 +279,7 @@ int upload_real(mkg_sim *s, const double *src, long long n, void *dst)
     if (r) return r;
     CK(s, cudaMemcpyAsync(s->d_stage, src, n * sizeof(double),
                           cudaMemcpyHostToDevice, s->stream));
+    s->n_launches++;
     k_convert<Real><<<grid_for(n), 256, 0, s->stream>>>(s->d_stage,
                                                        (Real *)dst, n);
     CK(s, cudaGetLastError());
@@ -913,6 +917,7 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
         }
         CK(s, cudaLaunchKernelExC(&lc, (const void *)s->kernel, args));
         s->last_launches++;
+        s->n_launches++;
         CK(s, cudaMemcpyAsync(s->h_status, s->d_status, sizeof(mkg_status),
                               cudaMemcpyDeviceToHost, s->stream));
         CK(s, cudaStreamSynchronize(s->stream));
@@ -941,6 +946,7 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
         if (s->h_steps[i].log_row >= 0) rows_done = s->h_steps[i].log_row + 1;
     if (rows_done > 0 && s->log_ncol > 0) {
         const long long cnt = rows_done * (long long)s->log_ncol;
+        s->n_launches++;
         if (s->real == 4)
             k_log_to_double<float><<<grid_for(cnt), 256, 0, s->stream>>>(
                 (const float *)s->d_log, s->d_log_dbl, cnt);
@@ -992,6 +998,20 @@ int mkg_last_stats(const mkg_sim *s, double *kernel_ms, int64_t *launches,
     if (kernel_ms) *kernel_ms = s->last_ms;
     if (launches) *launches = s->last_launches;
     if (cell_steps) *cell_steps = s->last_cell_steps;
+    return MKG_OK;
+}
+
+int mkg_launch_count(const mkg_sim *s, int64_t *count)
+{
+    if (!s || !count) return set_err(nullptr, MKG_ERR_ARG, "null argument");
+    *count = s->n_launches;
+    return MKG_OK;
+}
+
+int mkg_stream(const mkg_sim *s, void **stream)
+{
+    if (!s || !stream) return set_err(nullptr, MKG_ERR_ARG, "null argument");
+    *stream = (void *)s->stream;
     return MKG_OK;
 }
 

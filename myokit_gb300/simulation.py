@@ -900,6 +900,8 @@ class SimulationCUDA(object):
     def _execute(self, be, kernel, log, sources, tmin, tmax, log_interval,
                  progress, msg, duration):
         lib, h = be.lib, be.h
+        n0 = _lib.ctypes.c_int64()
+        lib.mkg_launch_count(h, _lib.ctypes.byref(n0))
         self._upload(be)
         cols = [(s[0], s[1]) for s in sources if len(s) == 2]
         items = np.ascontiguousarray([c[0] for c in cols], dtype=np.int32)
@@ -979,9 +981,11 @@ class SimulationCUDA(object):
         be.check(lib.mkg_get_state(h, _lib.dptr(st), st.size))
         self._state = st
 
+        n1 = _lib.ctypes.c_int64()
+        lib.mkg_launch_count(h, _lib.ctypes.byref(n1))
         self._last_stats = {
             'kernel_ms': ms_total, 'launches': launches,
-            'cell_steps': cell_steps,
+            'cell_steps': cell_steps, 'all_launches': n1.value - n0.value,
         }
 
         # Append to the log
@@ -998,6 +1002,18 @@ class SimulationCUDA(object):
                     data = vv[:, c]
                 _extend(log[key], data)
         return status == _lib.MKG_HALT_NAN
+
+    def cuda_stream(self):
+        """
+        The CUDA stream (an integer handle) the last run was queued on, or
+        ``None`` before the first run.
+        """
+        if self._backend is None:
+            return None
+        ptr = _lib.ctypes.c_void_p()
+        be = self._backend[1]
+        be.check(be.lib.mkg_stream(be.h, _lib.ctypes.byref(ptr)))
+        return ptr.value
 
     def last_run_stats(self):
         """
