@@ -123,7 +123,7 @@ class SimulationCUDA(object):
     def __init__(
             self, model, protocol=None, ncells=256, diffusion=True,
             precision=myokit.SINGLE_PRECISION, native_maths=False, rl=False,
-            block=None, steps_per_launch=0, device=0):
+            block=None, steps_per_launch=0, device=0, min_blocks=None):
 
         # Model checks (openclsim.py:155-167)
         if not model.is_valid():
@@ -224,6 +224,7 @@ class SimulationCUDA(object):
 
         # GPU options
         self._block = block
+        self._min_blocks = min_blocks
         self._steps_per_launch = int(steps_per_launch)
         self._device = int(device)
         self._backend = None
@@ -586,6 +587,13 @@ class SimulationCUDA(object):
         o = self._cell_offset(x, y, 'Y-coordinate')
         return self._state[o:o + self._nstate].tolist()
 
+    def state_array(self):
+        """
+        The current state as a float64 numpy array (a copy), laid out as
+        :meth:`state`; avoids building a Python list for large grids.
+        """
+        return np.array(self._state, dtype=float)
+
     def default_state(self, x=None, y=None):
         """The default state, indexed as :meth:`state`."""
         if x is None:
@@ -698,6 +706,13 @@ class SimulationCUDA(object):
             return (bx * by, 1)
         return (bx, by)
 
+    def _default_min_blocks(self, block):
+        """Minimum resident CTAs per SM asked of the compiler, which caps
+        the registers per thread at 64K / (threads * min_blocks)."""
+        if self._min_blocks is not None:
+            return int(self._min_blocks)
+        return 1
+
     def _kernel(self, inter_log):
         """The generated kernel for the current configuration."""
         mode = self._diffusion_mode()
@@ -707,7 +722,8 @@ class SimulationCUDA(object):
         return _exp.TissueKernel(
             self._model, self._precision, self._native_math,
             self._bound_variables, inter_log, mode, two_d,
-            list(self._fields.keys()), self._rl_states, block)
+            list(self._fields.keys()), self._rl_states, block,
+            min_blocks=self._default_min_blocks(block))
 
     def _get_backend(self, kernel):
         """A host-library handle for this kernel, reused between runs."""

@@ -245,7 +245,7 @@ def test_sheet512_rows_equal_cable(decker, precision):
     keys = ['%d.%d.membrane.V' % (x, y) for x in (0, 5, 100, 511)
             for y in (0, 1, 255, 511)]
     d = s.run(3, log=keys, log_interval=0.5)
-    st = np.array(s.state()).reshape(n, n, -1)
+    st = s.state_array().reshape(n, n, -1)
     assert np.all(np.isfinite(st))
     assert np.array_equal(st, np.broadcast_to(st[:1], st.shape))
     p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
@@ -253,7 +253,7 @@ def test_sheet512_rows_equal_cable(decker, precision):
     c.set_conductance(10)
     c.set_paced_cells(4)
     c.run(3)
-    assert np.array_equal(np.array(c.state()).reshape(n, -1), st[0])
+    assert np.array_equal(c.state_array().reshape(n, -1), st[0])
     for x in (0, 5, 100, 511):
         ref = np.asarray(d['%d.0.membrane.V' % x])
         for y in (1, 255, 511):
@@ -269,7 +269,7 @@ def test_sheet512_deterministic(decker):
         s = _sheet(decker, 512, SP)
         s.set_field('ikr.Gbar', f)
         s.run(2)
-        out.append(np.array(s.state()))
+        out.append(s.state_array())
     assert np.array_equal(out[0], out[1])
 
 
@@ -308,6 +308,6 @@ def test_sheet2048_runs(decker):
     d = s.run(0.1, log=['engine.time', '0.0.membrane.V',
                         '2047.2047.membrane.V'], log_interval=0.05)
     assert len(d['engine.time']) == 2
-    st = np.array(s.state()).reshape(2048, 2048, -1)
+    st = s.state_array().reshape(2048, 2048, -1)
     assert np.all(np.isfinite(st))
     assert np.array_equal(st[0], st[2047])
