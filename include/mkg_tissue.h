@@ -113,6 +113,31 @@ const char *mkg_last_error(const mkg_sim *sim);
 int mkg_set_state(mkg_sim *sim, const double *state, int64_t n);
 int mkg_get_state(mkg_sim *sim, double *state, int64_t n);
 
+/*
+ * mkg_set_state, without any allocation. No counterpart in the reference:
+ * its CPython module always allocates (openclsim.c uses malloc and
+ * clCreateBuffer per run).
+ *
+ * mkg_set_state stages the doubles in a device buffer that the handle
+ * allocates with cudaMalloc the first time. Callers that cannot call
+ * cudaMalloc at the point where they upload a state -- while a stream is
+ * being captured into a CUDA graph, or in a real-time pacing loop that
+ * must not suffer cudaMalloc's device-wide synchronisation -- use this call:
+ * it stages through a fixed 16 MiB array in the library's device image
+ * (held on every GPU that loads the library until the process exits) and
+ * calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * - n must equal nx*ny*n_state and be at most 2,097,152 (16 MiB of
+ *   doubles); larger states are rejected with MKG_ERR_ARG.
+ * - The first call on a device looks up the array's device address
+ *   (cudaGetSymbolAddress, with that device made current and then restored);
+ *   make that first call before any stream capture.
+ * - All handles share the array, which keeps the last call's contents;
+ *   each call overwrites the part it uses before reading it. Calls whose
+ *   GPU work overlaps (different streams, no ordering) race on it.
+ */
+int mkg_set_state_static(mkg_sim *sim, const double *state, int64_t n);
+
 /* Scalar fields, cell-major interleaved: field_data[cell*n_field + k]
  * (openclsim.py:1082-1089, openclsim.cl:201). n = nx*ny*n_field. */
 int mkg_set_fields(mkg_sim *sim, const double *field_data, int64_t n);

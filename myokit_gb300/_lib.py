@@ -66,6 +66,8 @@ SIGNATURES = {
     'mkg_last_error': (ctypes.c_char_p, [ctypes.c_void_p]),
     'mkg_set_state': (ctypes.c_int, [
         ctypes.c_void_p, _c_double_p, ctypes.c_int64]),
+    'mkg_set_state_static': (ctypes.c_int, [
+        ctypes.c_void_p, _c_double_p, ctypes.c_int64]),
     'mkg_get_state': (ctypes.c_int, [
         ctypes.c_void_p, _c_double_p, ctypes.c_int64]),
     'mkg_set_fields': (ctypes.c_int, [

@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <mutex>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -1042,3 +1043,117 @@ int64_t mkg_schedule_preview(const double *events, int64_t n_events,
 }
 
 }  /* extern "C" */
+
+/* ------------------------------------------------------------------------ */
+/* State upload without allocation                                          */
+/* ------------------------------------------------------------------------ */
+/*
+ * mkg_set_state stages the caller's doubles in a device buffer that the
+ * handle allocates with cudaMalloc on first use. Some callers cannot allow
+ * that call at that moment: code that uploads a new state inside a region
+ * being captured into a CUDA graph (cudaMalloc is not stream-ordered and
+ * breaks the capture), or a host loop driving pacing in real time, where
+ * cudaMalloc's implicit device-wide synchronisation stalls every stream.
+ * mkg_set_state_static stages through the fixed array below instead.
+ *
+ * The array lives in the library's device image: every GPU on which the
+ * library's module is loaded holds these MKG_STATIC_STAGE_BYTES until the
+ * process exits. Every call, from every handle, shares it and it keeps the
+ * last call's contents; the whole used range is overwritten by each call's
+ * copy before the conversion kernel reads it, so nothing needs clearing.
+ * Calls whose work overlaps on the GPU (different streams, no ordering
+ * between them) race on the array.
+ */
+#define MKG_STATIC_STAGE_DOUBLES (2ll * 1024 * 1024)   /* 16 MiB */
+
+static __device__ __align__(256) double
+    mkg_static_stage[MKG_STATIC_STAGE_DOUBLES];
+
+namespace {
+
+/* Same conversion as k_aos_to_soa, reading the fixed staging array. */
+template <typename Real>
+__global__ void k_aos_to_soa_static(Real *out, long long ncell, int nvar,
+                                    long long pitch, int skip_var, Real *alt)
+{
+    const long long n = ncell * nvar;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+         i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int s = (int)(i / ncell);
+        const long long c = i - (long long)s * ncell;
+        const Real v = (Real)mkg_static_stage[c * nvar + s];
+        if (s == skip_var) alt[c] = v;
+        else out[(long long)s * pitch + c] = v;
+    }
+}
+
+#define MKG_MAX_DEVICES 64
+std::mutex g_static_mutex;
+double *g_static_addr[MKG_MAX_DEVICES] = {nullptr};
+
+/* Device address of the staging array on the given device, looked up once
+ * per device with that device current. In host code the array's name is
+ * only a host-side stand-in, not a device address. */
+int static_stage_address(mkg_sim *s, double **addr)
+{
+    const int dev = s->cfg.device;
+    if (dev < 0 || dev >= MKG_MAX_DEVICES)
+        return set_err(s, MKG_ERR_ARG, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_addr[dev]) {
+        int prev = 0;
+        CK(s, cudaGetDevice(&prev));
+        CK(s, cudaSetDevice(dev));
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, mkg_static_stage);
+        cudaSetDevice(prev);
+        if (e != cudaSuccess)
+            return set_err(s, MKG_ERR_CUDA,
+                           "cudaGetSymbolAddress(mkg_static_stage) failed:"
+                           " %s", cudaGetErrorString(e));
+        g_static_addr[dev] = (double *)p;
+    }
+    *addr = g_static_addr[dev];
+    return MKG_OK;
+}
+
+template <typename Real>
+int upload_state_static(mkg_sim *s, const double *aos, double *stage)
+{
+    const int nvar = s->cfg.n_state;
+    const size_t bytes = (size_t)s->ncell * nvar * sizeof(double);
+    const int skip = diffusion_on(s) ? s->cfg.i_vm : -1;
+    Real *alt = (Real *)((char *)s->d_vbuf +
+                         (size_t)s->v_sel * s->pitch * s->real);
+    CK(s, cudaMemcpyAsync(stage, aos, bytes, cudaMemcpyHostToDevice,
+                          s->stream));
+    s->n_launches++;
+    k_aos_to_soa_static<Real><<<grid_for(s->ncell * nvar), 256, 0,
+                                 s->stream>>>(
+        (Real *)s->d_state, s->ncell, nvar, s->pitch, skip, alt);
+    CK(s, cudaGetLastError());
+    CK(s, cudaStreamSynchronize(s->stream));
+    return MKG_OK;
+}
+
+}  // namespace
+
+extern "C" int mkg_set_state_static(mkg_sim *s, const double *state,
+                                    int64_t n)
+{
+    if (!s || !state) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (n != s->ncell * s->cfg.n_state)
+        return set_err(s, MKG_ERR_ARG,
+                       "'state_in' must have size nx * ny * n_states.");
+    if (n > MKG_STATIC_STAGE_DOUBLES)
+        return set_err(s, MKG_ERR_ARG,
+                       "mkg_set_state_static: a state of %lld values exceeds"
+                       " the static staging area of %lld values (16 MiB);"
+                       " use mkg_set_state for this simulation",
+                       (long long)n, (long long)MKG_STATIC_STAGE_DOUBLES);
+    double *stage = nullptr;
+    const int r = static_stage_address(s, &stage);
+    if (r) return r;
+    if (s->real == 4) return upload_state_static<float>(s, state, stage);
+    return upload_state_static<double>(s, state, stage);
+}
