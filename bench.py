@@ -37,6 +37,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = 'cell-steps/s on 1 GB300 (FP32 vs FP64 at stated max|dV|)'
+
+# Single precision variants: FP64 or compensated accumulation of V and the
+# concentrations, and the fast FP32 arithmetic option
+VARIANTS = [
+    ('fp32+double', {'accumulate': 'double'}),
+    ('fp32+kahan', {'accumulate': 'kahan'}),
+    ('fp32-fast', {'fp32_math': 'fast'}),
+    ('fp32-fast+kahan', {'fp32_math': 'fast', 'accumulate': 'kahan'}),
+]
 UNIT = 'cell-steps/s'
 
 
@@ -50,6 +59,11 @@ def parse():
     p.add_argument('--step-ms', type=float, default=10.0)
     p.add_argument('--fp64-steps', type=int, default=2,
                    help='timed double precision bench steps (0 = skip)')
+    p.add_argument('--variant-steps', type=int, default=3,
+                   help='timed steps of the FP64/Kahan accumulation variants')
+    p.add_argument('--accuracy-ms', type=float, default=400.0,
+                   help='simulated time of the precision comparison runs'
+                        ' (0 = skip)')
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-seconds', type=float, default=12.0,
                    help='target CPU work for the cpu_baseline sample')
@@ -209,6 +223,67 @@ def cpu_baseline(args, precision, seconds):
     }
 
 
+def accuracy_runs(args, device):
+    """
+    Precision comparison over a full action potential: max |dV|, activation
+    time and APD90 errors at probe cells of (a) a 128x128 sheet against its
+    FP64 run on the GPU and (b) a 24x24 sheet against the FP64 CPU oracle
+    (the reference's kernel), both with the bench sheet's configuration.
+    """
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+    from myokit_gb300 import metrics
+    from oracle.refsim import ReferenceCpuSimulation
+    modes = [('fp32', {})] + list(VARIANTS)
+    out = {}
+
+    def probes(n, k, seed):
+        rng = np.random.default_rng(seed)
+        cells = sorted(rng.choice(n * n, k, replace=False))
+        return ['%d.%d.membrane.V' % (c % n, c // n) for c in cells]
+
+    def traces(d, keys):
+        return {k: np.asarray(d[k], dtype=float) for k in keys}
+
+    # (a) 128 x 128 against FP64 on the GPU
+    n = 128
+    keys = probes(n, 64, 1)
+    log = ['engine.time'] + keys
+    s, _ = make_sheet(mg.SimulationCUDA, myokit.DOUBLE_PRECISION, n,
+                      device=device)
+    ref = s.run(args.accuracy_ms, log=log, log_interval=0.5)
+    t = np.asarray(ref['engine.time'])
+    res = {}
+    for name, kw in modes:
+        s, _ = make_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION, n,
+                          device=device, **kw)
+        d = s.run(args.accuracy_ms, log=log, log_interval=0.5)
+        res[name] = metrics.compare(t, traces(d, keys), traces(ref, keys))
+    out['sheet128_vs_fp64_gpu'] = dict(res, window_ms=args.accuracy_ms,
+                                       probes=len(keys))
+
+    # (b) 24 x 24 against the FP64 CPU oracle
+    n = 24
+    keys = probes(n, 32, 2)
+    log = ['engine.time'] + keys
+    so, _ = make_sheet(ReferenceCpuSimulation, myokit.DOUBLE_PRECISION, n)
+    so.set_threads(os.cpu_count() or 1)
+    ref = so.run(args.accuracy_ms, log=log, log_interval=0.5)
+    t = np.asarray(ref['engine.time'])
+    res = {}
+    for name, kw in [('fp64', {'precision': myokit.DOUBLE_PRECISION})] + [
+            (m, dict(k, precision=myokit.SINGLE_PRECISION))
+            for m, k in modes]:
+        kw = dict(kw)
+        prec = kw.pop('precision')
+        s, _ = make_sheet(mg.SimulationCUDA, prec, n, device=device, **kw)
+        d = s.run(args.accuracy_ms, log=log, log_interval=0.5)
+        res[name] = metrics.compare(t, traces(d, keys), traces(ref, keys))
+    out['sheet24_vs_fp64_oracle'] = dict(res, window_ms=args.accuracy_ms,
+                                         probes=len(keys))
+    return out
+
+
 def run_reference(args):
     """--impl reference: the reference kernel on the host cores."""
     rank = int(os.environ.get('RANK', '0'))
@@ -366,6 +441,35 @@ def run_ours(args):
               'against': 'this sheet in double precision on the GPU'}
         fp64['speedup_fp32_over_fp64'] = value / world / fp64['value']
 
+    # --- single precision with FP64 / Kahan accumulation --------------------
+    variants = {}
+    if args.variant_steps > 0 and rank == 0:
+        for vname, kw in VARIANTS:
+            sv, _ = make_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION,
+                               args.size, seed=rank, device=local, **kw)
+            dms = 0.0
+            ncs = 0
+            for i in range(args.warmup + args.variant_steps):
+                flush.fill_(1)
+                torch.cuda.synchronize()
+                sv.run(args.step_ms, log=log, log_interval=1)
+                if i >= args.warmup:
+                    st = sv.last_run_stats()
+                    dms += st['kernel_ms']
+                    ncs += st['cell_steps']
+            v = ncs / (dms / 1000.0)
+            variants[vname] = {
+                'value': v, 'unit': UNIT,
+                'accumulated_states': [x.qname()
+                                       for x in sv.accumulated_states()],
+                'bytes_per_cell_step': sv._last_kernel.bytes_per_cell_step(),
+                'speedup_over_fp64': (v / fp64['value']) if fp64 else None,
+            }
+
+    accuracy = {'fp32_vs_fp64_bench_sheet': dv}
+    if args.accuracy_ms > 0 and rank == 0:
+        accuracy.update(accuracy_runs(args, local))
+
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline(args, myokit.SINGLE_PRECISION, args.cpu_seconds)
@@ -397,7 +501,8 @@ def run_ours(args):
                 'peak_source': 'FP32 lanes x 2 x median SM clock'},
         },
         'fp64': fp64,
-        'accuracy': dv,
+        'variants': variants,
+        'accuracy': accuracy,
         'clocks': clocks,
         'cpu_baseline': cpu,
     }

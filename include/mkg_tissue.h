@@ -78,6 +78,10 @@ typedef struct mkg_config {
     int32_t two_d;          /* 1: kernel tiles an (nx, ny) grid with
                                (block_x, block_y) CTAs; 0: cells are a
                                flat array covered by (block_x, 1) CTAs */
+    int32_t hi_mode;        /* single precision only: 0 none, 1 selected
+                               states stored and updated in FP64, 2 selected
+                               states carry an FP32 Kahan compensation term */
+    int32_t n_hi;           /* number of selected states (mkg_set_hi_states) */
 } mkg_config;
 
 /*
@@ -107,6 +111,12 @@ void mkg_destroy(mkg_sim *sim);
 /* Last error message for this handle, or for the calling thread when sim is
  * NULL. Never returns NULL. */
 const char *mkg_last_error(const mkg_sim *sim);
+
+/* The states kept in the accumulation planes when cfg.hi_mode != 0, in
+ * plane order (n == cfg.n_hi). Must be called before mkg_set_state. No
+ * counterpart in the reference, which stores every state in one precision
+ * (openclsim.cl:158-169). */
+int mkg_set_hi_states(mkg_sim *sim, const int32_t *states, int32_t n);
 
 /* Cell state, AoS doubles, n = nx*ny*n_state (state_in, openclsim.c:512-521;
  * state_out, openclsim.c:1185-1190). */
@@ -196,10 +206,13 @@ int mkg_run_chunk(mkg_sim *sim, int64_t max_steps, double *t_out,
 int mkg_read_log(mkg_sim *sim, double *time, double *pace, double *values,
                  int64_t rows);
 
-/* Launch tuning: steps fused into one launch (0 = automatic) and blocks per
- * SM for the persistent grid (0 = occupancy maximum). */
+/* Launch tuning: steps fused into one launch (0 = the whole chunk in one
+ * cooperative launch; 1 = one plain launch per step, no grid barrier),
+ * blocks per SM for the cooperative grid (0 = occupancy maximum), and
+ * whether a chunk's launches are captured once as a CUDA graph and
+ * replayed (use_graphs != 0). */
 int mkg_set_tuning(mkg_sim *sim, int32_t steps_per_launch,
-                   int32_t blocks_per_sm);
+                   int32_t blocks_per_sm, int32_t use_graphs);
 
 /* Timing and counters of the last chunk: device milliseconds spent in
  * step kernels, number of kernel launches and cell-steps computed. */

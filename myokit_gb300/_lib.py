@@ -49,6 +49,8 @@ class MkgConfig(ctypes.Structure):
         ('block_y', ctypes.c_int32),
         ('device', ctypes.c_int32),
         ('two_d', ctypes.c_int32),
+        ('hi_mode', ctypes.c_int32),
+        ('n_hi', ctypes.c_int32),
     ]
 
 
@@ -66,6 +68,8 @@ SIGNATURES = {
     'mkg_last_error': (ctypes.c_char_p, [ctypes.c_void_p]),
     'mkg_set_state': (ctypes.c_int, [
         ctypes.c_void_p, _c_double_p, ctypes.c_int64]),
+    'mkg_set_hi_states': (ctypes.c_int, [
+        ctypes.c_void_p, _c_int32_p, ctypes.c_int32]),
     'mkg_set_state_static': (ctypes.c_int, [
         ctypes.c_void_p, _c_double_p, ctypes.c_int64]),
     'mkg_get_state': (ctypes.c_int, [
@@ -100,7 +104,7 @@ SIGNATURES = {
         ctypes.c_void_p, _c_double_p, _c_double_p, _c_double_p,
         ctypes.c_int64]),
     'mkg_set_tuning': (ctypes.c_int, [
-        ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+        ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     'mkg_last_stats': (ctypes.c_int, [
         ctypes.c_void_p, _c_double_p, _c_int64_p, _c_int64_p]),
     'mkg_launch_count': (ctypes.c_int, [ctypes.c_void_p, _c_int64_p]),

@@ -1,0 +1,148 @@
+"""
+Launch-shape autotuner for :class:`SimulationCUDA`.
+
+The fused kernel's speed depends on the CTA shape (which sets the tile of
+cells that shares one shared-memory V halo), on the register cap that the
+minimum number of resident CTAs per SM implies, and on how steps are
+grouped into launches (one cooperative launch per chunk with a grid barrier
+between steps, or one plain launch per step replayed from a CUDA graph).
+:func:`autotune` times candidates on the simulation itself -- same model,
+grid, fields and precision -- and keeps the fastest. Results are cached per
+configuration signature in ``<cache dir>/tune.json``; a simulation created
+with ``block=None`` uses a cached result when one matches.
+"""
+import json
+import os
+import time
+
+import numpy as np
+
+from ._deps import myokit
+
+# Candidate (block, min CTAs per SM, steps per launch)
+_CANDIDATES_2D = [
+    ((64, 4), 2, 0), ((32, 8), 2, 0), ((32, 4), 4, 0), ((32, 4), 1, 0),
+    ((64, 2), 4, 0), ((32, 6), 3, 0), ((64, 4), 2, 1), ((32, 4), 4, 1),
+]
+_CANDIDATES_1D = [
+    ((256, 1), 2, 0), ((128, 1), 4, 0), ((128, 1), 1, 0), ((192, 1), 3, 0),
+    ((64, 1), 8, 0), ((256, 1), 2, 1), ((128, 1), 4, 1),
+]
+
+
+def _cache_path():
+    from .simulation import _cache_dir
+    return os.path.join(_cache_dir(), 'tune.json')
+
+
+def _shipped_path():
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                        'tuned.json')
+
+
+def signature(sim):
+    """A string identifying what the best launch shape depends on."""
+    import hashlib
+    code = hashlib.sha1(sim._model.code().encode()).hexdigest()[:16]
+    return '|'.join(str(x) for x in (
+        sim._model.name(), code, sim._nx, sim._ny, len(sim._dims),
+        sim._precision, sim._accumulate, sim._diffusion_mode(),
+        ','.join(v.qname() for v in sim._fields), len(sim._rl_states),
+        sim._fp32_math, sim._native_math))
+
+
+def _load(path):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def lookup(sim):
+    """The cached choice for this simulation's signature, or None."""
+    sig = signature(sim)
+    for path in (_cache_path(), _shipped_path()):
+        d = _load(path)
+        if sig in d:
+            return d[sig]
+    return None
+
+
+def _apply(sim, block, min_blocks, spl):
+    sim._block = tuple(block)
+    sim._min_blocks = int(min_blocks)
+    sim._steps_per_launch = int(spl)
+    sim._graphs = 1
+
+
+def autotune(sim, duration=None, candidates=None, store=True,
+             verbose=False):
+    """
+    Times each candidate launch configuration on ``sim`` for ``duration``
+    time units (default: about 4e8 cell-steps) without logging, restores the
+    simulation's state and time, applies the fastest configuration and
+    returns ``(best, results)``. ``results`` maps each candidate to its
+    cell-steps per second of device time.
+    """
+    two_d = len(sim._dims) == 2 and sim._diffusion_enabled and \
+        sim._connections is None
+    if candidates is None:
+        candidates = _CANDIDATES_2D if two_d else _CANDIDATES_1D
+        if sim._precision == myokit.DOUBLE_PRECISION:
+            # FP64 kernels spill when registers are capped
+            candidates = [c for c in candidates if c[1] == 1] or [
+                ((32, 4) if two_d else (128, 1), 1, 0)]
+    if duration is None:
+        steps = max(20, int(4e8 / sim._ntotal))
+        if sim._precision == myokit.DOUBLE_PRECISION:
+            steps = max(4, steps // 20)
+        duration = steps * sim.step_size()
+    saved = (sim._state.copy(), sim._time, sim._block, sim._min_blocks,
+             sim._steps_per_launch, sim._graphs)
+    results = {}
+    try:
+        for cand in candidates:
+            block, mb, spl = cand
+            _apply(sim, block, mb, spl)
+            sim._state = saved[0].copy()
+            sim._time = saved[1]
+            try:
+                sim._run(duration / 4, myokit.LOG_NONE, 1, False, None, '')
+                sim._state = saved[0].copy()
+                sim._run(duration, myokit.LOG_NONE, 1, False, None, '')
+            except Exception as e:   # pragma: no cover
+                if verbose:
+                    print('autotune: %s failed: %s' % (cand, e))
+                continue
+            st = sim.last_run_stats()
+            rate = st['cell_steps'] / (st['kernel_ms'] / 1000.0)
+            results[cand] = rate
+            if verbose:
+                print('autotune: block=%s min_blocks=%d steps/launch=%d'
+                      ' -> %.4g cell-steps/s' % (block, mb, spl, rate))
+    finally:
+        sim._state, sim._time = saved[0], saved[1]
+        sim._block, sim._min_blocks = saved[2], saved[3]
+        sim._steps_per_launch, sim._graphs = saved[4], saved[5]
+    if not results:
+        return None, results
+    best = max(results, key=results.get)
+    _apply(sim, *best)
+    sim._tuned = True
+    if store:
+        path = _cache_path()
+        d = _load(path)
+        d[signature(sim)] = {
+            'block': list(best[0]), 'min_blocks': best[1],
+            'steps_per_launch': best[2], 'rate': results[best],
+            'when': time.strftime('%Y-%m-%dT%H:%M:%S')}
+        try:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            tmp = path + '.%d' % os.getpid()
+            with open(tmp, 'w') as f:
+                json.dump(d, f, indent=1, sort_keys=True)
+            os.replace(tmp, path)
+        except OSError:   # pragma: no cover
+            pass
+    return best, results

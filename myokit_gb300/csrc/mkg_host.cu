@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <map>
 #include <mutex>
 #include <cstdarg>
 #include <cstdio>
@@ -34,6 +35,9 @@
 #include "mkg_kernel_abi.h"
 #include "mkg_pacing.h"
 
+/* Shared memory per CTA for staged V tiles (2D kernels) */
+#define MKG_STAGE_BUDGET 24576
+
 namespace {
 
 thread_local std::string g_thread_error;
@@ -42,21 +46,44 @@ thread_local std::string g_thread_error;
 /* Fixed device kernels                                                     */
 /* ------------------------------------------------------------------------ */
 
-/* AoS doubles [ncell][nvar] -> SoA Real [nvar][pitch]; variable skip_var
- * (if >= 0) goes to alt instead (the V ping-pong plane). */
+/* Where a state lives on the device */
+struct Slots {
+    int skip_var;        /* state held in the V plane (alt), or -1 */
+    int v_double;        /* the V plane holds doubles */
+    int hi_mode;         /* MKG_HI_* */
+    const int *hi_slot;  /* per state: accumulation plane, or -1 (or null) */
+    void *hi;            /* accumulation planes [n_hi][pitch] */
+};
+
+/* AoS doubles [ncell][nvar] -> SoA Real [nvar][pitch]. The V state goes to
+ * the V plane (alt); states with an accumulation plane go there as FP64, or
+ * (Kahan) as an FP32 value x plus a term c with x - c equal to the double. */
 template <typename Real>
 __global__ void k_aos_to_soa(const double *__restrict__ in, Real *out,
                              long long ncell, int nvar, long long pitch,
-                             int skip_var, Real *alt)
+                             Slots sl, void *alt)
 {
     const long long n = ncell * nvar;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
          i < n; i += (long long)gridDim.x * blockDim.x) {
         const int s = (int)(i / ncell);
         const long long c = i - (long long)s * ncell;
-        const Real v = (Real)in[c * nvar + s];
-        if (s == skip_var) alt[c] = v;
-        else out[(long long)s * pitch + c] = v;
+        const double v = in[c * nvar + s];
+        const int j = sl.hi_slot ? sl.hi_slot[s] : -1;
+        if (j >= 0 && sl.hi_mode == MKG_HI_DOUBLE) {
+            if (s == sl.skip_var) ((double *)alt)[c] = v;
+            else ((double *)sl.hi)[(long long)j * pitch + c] = v;
+            continue;
+        }
+        const Real x = (Real)v;
+        if (s == sl.skip_var) {
+            if (sl.v_double) ((double *)alt)[c] = v;
+            else ((Real *)alt)[c] = x;
+        } else {
+            out[(long long)s * pitch + c] = x;
+        }
+        if (j >= 0 && sl.hi_mode == MKG_HI_KAHAN)
+            ((Real *)sl.hi)[(long long)j * pitch + c] = (Real)((double)x - v);
     }
 }
 
@@ -64,15 +91,25 @@ __global__ void k_aos_to_soa(const double *__restrict__ in, Real *out,
 template <typename Real>
 __global__ void k_soa_to_aos(const Real *__restrict__ in, double *out,
                              long long ncell, int nvar, long long pitch,
-                             int skip_var, const Real *alt)
+                             Slots sl, const void *alt)
 {
     const long long n = ncell * nvar;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
          i < n; i += (long long)gridDim.x * blockDim.x) {
         const int s = (int)(i / ncell);
         const long long c = i - (long long)s * ncell;
-        const Real v = (s == skip_var) ? alt[c] : in[(long long)s * pitch + c];
-        out[c * nvar + s] = (double)v;
+        const int j = sl.hi_slot ? sl.hi_slot[s] : -1;
+        double v;
+        if (s == sl.skip_var)
+            v = sl.v_double ? ((const double *)alt)[c]
+                            : (double)((const Real *)alt)[c];
+        else if (j >= 0 && sl.hi_mode == MKG_HI_DOUBLE)
+            v = ((const double *)sl.hi)[(long long)j * pitch + c];
+        else
+            v = (double)in[(long long)s * pitch + c];
+        if (j >= 0 && sl.hi_mode == MKG_HI_KAHAN)
+            v -= (double)((const Real *)sl.hi)[(long long)j * pitch + c];
+        out[c * nvar + s] = v;
     }
 }
 
@@ -119,6 +156,7 @@ struct mkg_sim {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t kernel = nullptr;
     int occ_blocks = 1;       /* co-resident blocks per SM */
+    int stage_budget = 0;     /* dynamic shared memory per CTA (bytes) */
     int num_sms = 1;
 
     /* device buffers */
@@ -135,6 +173,10 @@ struct mkg_sim {
     mkg_step *d_steps = nullptr;
     mkg_status *d_status = nullptr;
     double *d_stage = nullptr;   /* staging for double uploads */
+    void *d_hi = nullptr;        /* accumulation planes [n_hi][pitch] x 8 B */
+    int *d_hi_slot = nullptr;    /* per state: accumulation plane or -1 */
+    int v_double = 0;            /* V plane holds doubles */
+    int vbytes = 4;              /* bytes per V plane entry */
     size_t stage_bytes = 0;
 
     /* pinned host buffers */
@@ -165,6 +207,8 @@ struct mkg_sim {
     double last_ms = 0;
     int64_t last_launches = 0, last_cell_steps = 0;
     int64_t n_launches = 0;   /* every kernel launched by this handle */
+    bool use_graphs = false;  /* replay multi-launch chunks as CUDA graphs */
+    std::map<std::string, cudaGraphExec_t> graphs;
 };
 
 namespace {
@@ -207,8 +251,16 @@ int ensure_stage(mkg_sim *s, size_t bytes)
     return MKG_OK;
 }
 
+/* Cached graphs bake in buffer pointers and launch parameters */
+void clear_graphs(mkg_sim *s)
+{
+    for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
+    s->graphs.clear();
+}
+
 int ensure_schedule(mkg_sim *s, int64_t steps, int64_t rows)
 {
+    if (steps > s->cap_steps || rows > s->cap_rows) clear_graphs(s);
     if (steps > s->cap_steps) {
         dfree(s->d_steps);
         if (s->h_steps) cudaFreeHost(s->h_steps);
@@ -236,9 +288,31 @@ int ensure_schedule(mkg_sim *s, int64_t steps, int64_t rows)
     return MKG_OK;
 }
 
+Slots state_slots(const mkg_sim *s)
+{
+    Slots sl;
+    sl.skip_var = s->cfg.diffusion != MKG_DIFF_NONE ? s->cfg.i_vm : -1;
+    sl.v_double = s->v_double;
+    sl.hi_mode = s->cfg.hi_mode;
+    sl.hi_slot = s->d_hi_slot;
+    sl.hi = s->d_hi;
+    return sl;
+}
+
+Slots plain_slots()
+{
+    Slots sl;
+    sl.skip_var = -1;
+    sl.v_double = 0;
+    sl.hi_mode = MKG_HI_NONE;
+    sl.hi_slot = nullptr;
+    sl.hi = nullptr;
+    return sl;
+}
+
 template <typename Real>
-int upload_soa(mkg_sim *s, const double *aos, int nvar, void *dst,
-               int skip_var, void *alt)
+int upload_soa(mkg_sim *s, const double *aos, int nvar, void *dst, Slots sl,
+               void *alt)
 {
     const size_t bytes = (size_t)s->ncell * nvar * sizeof(double);
     int r = ensure_stage(s, bytes);
@@ -247,8 +321,7 @@ int upload_soa(mkg_sim *s, const double *aos, int nvar, void *dst,
                           s->stream));
     s->n_launches++;
     k_aos_to_soa<Real><<<grid_for(s->ncell * nvar), 256, 0, s->stream>>>(
-        s->d_stage, (Real *)dst, s->ncell, nvar, s->pitch, skip_var,
-        (Real *)alt);
+        s->d_stage, (Real *)dst, s->ncell, nvar, s->pitch, sl, alt);
     CK(s, cudaGetLastError());
     CK(s, cudaStreamSynchronize(s->stream));
     return MKG_OK;
@@ -256,15 +329,14 @@ int upload_soa(mkg_sim *s, const double *aos, int nvar, void *dst,
 
 template <typename Real>
 int download_soa(mkg_sim *s, double *aos, int nvar, const void *src,
-                 int skip_var, const void *alt)
+                 Slots sl, const void *alt)
 {
     const size_t bytes = (size_t)s->ncell * nvar * sizeof(double);
     int r = ensure_stage(s, bytes);
     if (r) return r;
     s->n_launches++;
     k_soa_to_aos<Real><<<grid_for(s->ncell * nvar), 256, 0, s->stream>>>(
-        (const Real *)src, s->d_stage, s->ncell, nvar, s->pitch, skip_var,
-        (const Real *)alt);
+        (const Real *)src, s->d_stage, s->ncell, nvar, s->pitch, sl, alt);
     CK(s, cudaGetLastError());
     CK(s, cudaMemcpyAsync(aos, s->d_stage, bytes, cudaMemcpyDeviceToHost,
                           s->stream));
@@ -384,6 +456,7 @@ void mkg_destroy(mkg_sim *s)
 {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    clear_graphs(s);
     dfree(s->d_state);
     dfree(s->d_vbuf);
     dfree(s->d_field);
@@ -400,6 +473,8 @@ void mkg_destroy(mkg_sim *s)
     dfree(s->d_steps);
     dfree(s->d_status);
     dfree(s->d_stage);
+    dfree(s->d_hi);
+    dfree(s->d_hi_slot);
     if (s->h_steps) cudaFreeHost(s->h_steps);
     if (s->h_status) cudaFreeHost(s->h_status);
     if (s->h_log) cudaFreeHost(s->h_log);
@@ -425,6 +500,11 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
                        "Only single and double precision are supported.");
     if (cfg->n_state < 1 || cfg->n_field < 0 || cfg->n_inter < 0)
         return set_err(nullptr, MKG_ERR_ARG, "invalid variable counts");
+    if (cfg->hi_mode < MKG_HI_NONE || cfg->hi_mode > MKG_HI_KAHAN ||
+        cfg->n_hi < 0 || cfg->n_hi > cfg->n_state ||
+        (cfg->hi_mode != MKG_HI_NONE && cfg->real_bytes != 4))
+        return set_err(nullptr, MKG_ERR_ARG,
+                       "invalid accumulation mode (single precision only)");
     if (cfg->diffusion < MKG_DIFF_NONE || cfg->diffusion > MKG_DIFF_CONN)
         return set_err(nullptr, MKG_ERR_ARG, "invalid diffusion mode");
     if (cfg->diffusion != MKG_DIFF_NONE &&
@@ -464,9 +544,12 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
     CKC(cudaLibraryGetKernel(&s->kernel, s->lib, "mkg_tissue_step"));
     CKC(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount,
                                cfg->device));
+    /* 2D kernels stage V tiles in dynamic shared memory, at most
+     * MKG_STAGE_BUDGET bytes per CTA; occupancy is computed for that. */
+    s->stage_budget = cfg->two_d ? MKG_STAGE_BUDGET : 0;
     CKC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &s->occ_blocks, (const void *)s->kernel,
-        cfg->block_x * cfg->block_y, 0));
+        cfg->block_x * cfg->block_y, s->stage_budget));
     if (s->occ_blocks < 1) {
         set_err(nullptr, MKG_ERR_CUDA,
                 "the generated kernel cannot be resident on an SM");
@@ -477,8 +560,18 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
     const size_t plane = (size_t)s->pitch * s->real;
     CKC(cudaMalloc(&s->d_state, plane * cfg->n_state));
     CKC(cudaMemsetAsync(s->d_state, 0, plane * cfg->n_state, s->stream));
-    CKC(cudaMalloc(&s->d_vbuf, plane * 2));
-    CKC(cudaMemsetAsync(s->d_vbuf, 0, plane * 2, s->stream));
+    /* V planes hold doubles when V is accumulated in FP64: 8 B entries */
+    CKC(cudaMalloc(&s->d_vbuf, (size_t)s->pitch * 8 * 2));
+    CKC(cudaMemsetAsync(s->d_vbuf, 0, (size_t)s->pitch * 8 * 2, s->stream));
+    s->vbytes = s->real;
+    if (cfg->hi_mode != MKG_HI_NONE && cfg->n_hi > 0) {
+        CKC(cudaMalloc(&s->d_hi, (size_t)s->pitch * 8 * cfg->n_hi));
+        CKC(cudaMemsetAsync(s->d_hi, 0, (size_t)s->pitch * 8 * cfg->n_hi,
+                            s->stream));
+        CKC(cudaMalloc((void **)&s->d_hi_slot, cfg->n_state * sizeof(int)));
+        CKC(cudaMemsetAsync(s->d_hi_slot, 0xff, cfg->n_state * sizeof(int),
+                            s->stream));
+    }
     if (cfg->n_field > 0) {
         CKC(cudaMalloc(&s->d_field, plane * cfg->n_field));
         CKC(cudaMemsetAsync(s->d_field, 0, plane * cfg->n_field, s->stream));
@@ -491,19 +584,42 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
     return MKG_OK;
 }
 
+int mkg_set_hi_states(mkg_sim *s, const int32_t *states, int32_t n)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (n != s->cfg.n_hi || (n > 0 && !states))
+        return set_err(s, MKG_ERR_ARG, "expected %d accumulated states",
+                       s->cfg.n_hi);
+    std::vector<int> slot(s->cfg.n_state, -1);
+    for (int j = 0; j < n; ++j) {
+        if (states[j] < 0 || states[j] >= s->cfg.n_state ||
+            slot[states[j]] >= 0)
+            return set_err(s, MKG_ERR_ARG, "invalid accumulated state %d",
+                           states[j]);
+        slot[states[j]] = j;
+    }
+    CK(s, cudaMemcpyAsync(s->d_hi_slot, slot.data(),
+                          slot.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          s->stream));
+    CK(s, cudaStreamSynchronize(s->stream));
+    s->v_double = (s->cfg.hi_mode == MKG_HI_DOUBLE && diffusion_on(s) &&
+                   slot[s->cfg.i_vm] >= 0) ? 1 : 0;
+    s->vbytes = s->v_double ? 8 : s->real;
+    return MKG_OK;
+}
+
 int mkg_set_state(mkg_sim *s, const double *state, int64_t n)
 {
     if (!s || !state) return set_err(s, MKG_ERR_ARG, "null argument");
     if (n != s->ncell * s->cfg.n_state)
         return set_err(s, MKG_ERR_ARG,
                        "'state_in' must have size nx * ny * n_states.");
-    const int skip = diffusion_on(s) ? s->cfg.i_vm : -1;
-    void *alt = (char *)s->d_vbuf + (size_t)s->v_sel * s->pitch * s->real;
+    void *alt = (char *)s->d_vbuf + (size_t)s->v_sel * s->pitch * s->vbytes;
     if (s->real == 4)
-        return upload_soa<float>(s, state, s->cfg.n_state, s->d_state, skip,
-                                 alt);
-    return upload_soa<double>(s, state, s->cfg.n_state, s->d_state, skip,
-                              alt);
+        return upload_soa<float>(s, state, s->cfg.n_state, s->d_state,
+                                 state_slots(s), alt);
+    return upload_soa<double>(s, state, s->cfg.n_state, s->d_state,
+                              state_slots(s), alt);
 }
 
 int mkg_get_state(mkg_sim *s, double *state, int64_t n)
@@ -512,14 +628,13 @@ int mkg_get_state(mkg_sim *s, double *state, int64_t n)
     if (n != s->ncell * s->cfg.n_state)
         return set_err(s, MKG_ERR_ARG,
                        "'state_out' must have size nx * ny * n_states.");
-    const int skip = diffusion_on(s) ? s->cfg.i_vm : -1;
     const void *alt =
-        (const char *)s->d_vbuf + (size_t)s->v_sel * s->pitch * s->real;
+        (const char *)s->d_vbuf + (size_t)s->v_sel * s->pitch * s->vbytes;
     if (s->real == 4)
-        return download_soa<float>(s, state, s->cfg.n_state, s->d_state, skip,
-                                   alt);
-    return download_soa<double>(s, state, s->cfg.n_state, s->d_state, skip,
-                                alt);
+        return download_soa<float>(s, state, s->cfg.n_state, s->d_state,
+                                   state_slots(s), alt);
+    return download_soa<double>(s, state, s->cfg.n_state, s->d_state,
+                                state_slots(s), alt);
 }
 
 int mkg_set_fields(mkg_sim *s, const double *field_data, int64_t n)
@@ -532,9 +647,9 @@ int mkg_set_fields(mkg_sim *s, const double *field_data, int64_t n)
     if (!field_data) return set_err(s, MKG_ERR_ARG, "null argument");
     if (s->real == 4)
         return upload_soa<float>(s, field_data, s->cfg.n_field, s->d_field,
-                                 -1, nullptr);
-    return upload_soa<double>(s, field_data, s->cfg.n_field, s->d_field, -1,
-                              nullptr);
+                                 plain_slots(), nullptr);
+    return upload_soa<double>(s, field_data, s->cfg.n_field, s->d_field,
+                              plain_slots(), nullptr);
 }
 
 int mkg_set_conductance(mkg_sim *s, double gx, double gy)
@@ -736,13 +851,15 @@ int mkg_set_log(mkg_sim *s, const int32_t *item, const int64_t *cell,
 }
 
 int mkg_set_tuning(mkg_sim *s, int32_t steps_per_launch,
-                   int32_t blocks_per_sm)
+                   int32_t blocks_per_sm, int32_t use_graphs)
 {
     if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
     if (steps_per_launch < 0 || blocks_per_sm < 0)
         return set_err(s, MKG_ERR_ARG, "invalid tuning");
+    clear_graphs(s);
     s->steps_per_launch = steps_per_launch;
     s->blocks_per_sm = blocks_per_sm;
+    s->use_graphs = use_graphs != 0;
     return MKG_OK;
 }
 
@@ -765,6 +882,7 @@ int mkg_run_begin(mkg_sim *s, double tmin, double tmax, double default_dt,
         int r = mkg_set_log(s, nullptr, nullptr, 0, 0);
         if (r) return r;
     }
+    clear_graphs(s);
     const int st = s->sched.begin(s->pacer, tmin, tmax, default_dt,
                                   log_interval);
     if (st != mkg::PACER_OK) return pacer_err(s, st);
@@ -866,6 +984,7 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
     a.nan_check = s->nan_check;
     a.status = s->d_status;
     a.timeout_ns = s->timeout_ns;
+    a.hi = s->d_hi;
     if (two_d) {
         a.ntiles_x = (int)((s->cfg.nx + bx - 1) / bx);
         a.ntiles_y = (int)((s->cfg.ny + by - 1) / by);
@@ -882,64 +1001,128 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
                                     : s->occ_blocks;
     long long coop_blocks = std::min<long long>(ntiles,
                                                 (long long)bpsm * s->num_sms);
+    /* Tiles staged per __syncthreads and the shared memory that takes */
+    const size_t tile_bytes = (size_t)(bx + 2) * (by + 2) * s->vbytes;
+    auto staging = [&](long long grid, int *stage_tiles, size_t *smem) {
+        const long long per = (ntiles + grid - 1) / grid;
+        if (!two_d) {
+            *stage_tiles = (int)std::min<long long>(per, INT_MAX);
+            *smem = 0;
+            return;
+        }
+        long long m = std::max<long long>(
+            1, std::min<long long>(per, s->stage_budget / tile_bytes));
+        *stage_tiles = (int)m;
+        *smem = (size_t)m * tile_bytes;
+    };
     int spl = s->steps_per_launch > 0 ? s->steps_per_launch : 1 << 20;
 
-    CK(s, cudaEventRecord(s->ev0, s->stream));
-    int64_t done = 0;
-    bool halted = false;
+    /* All launches of the chunk are queued without host synchronisation;
+     * the status word is reset once. Launch i covers steps
+     * [off_i, off_i + m_i); a NaN halt or device error makes every later
+     * launch return at once. */
     mkg_status init;
     init.barrier = 0;
     init.error = MKG_DEV_OK;
     init.halt_step = MKG_NO_HALT;
     init.timeout_block = -1;
-    while (done < n) {
-        const int64_t m = std::min<int64_t>(n - done, spl);
-        *s->h_status = init;
-        CK(s, cudaMemcpyAsync(s->d_status, s->h_status, sizeof(mkg_status),
-                              cudaMemcpyHostToDevice, s->stream));
-        a.steps = s->d_steps + done;
-        a.nsteps = (int)m;
-        a.v_sel = s->v_sel;
-        void *args[] = {&a};
-        cudaLaunchConfig_t lc;
-        memset(&lc, 0, sizeof(lc));
-        cudaLaunchAttribute attr[1];
-        lc.blockDim = dim3(bx, by, 1);
-        lc.stream = s->stream;
-        if (m > 1) {
-            lc.gridDim = dim3((unsigned)coop_blocks, 1, 1);
-            attr[0].id = cudaLaunchAttributeCooperative;
-            attr[0].val.cooperative = 1;
-            lc.attrs = attr;
-            lc.numAttrs = 1;
-        } else {
-            lc.gridDim = dim3((unsigned)std::min<long long>(ntiles, 1 << 30),
-                              1, 1);
+    *s->h_status = init;
+    CK(s, cudaMemcpyAsync(s->d_status, s->h_status, sizeof(mkg_status),
+                          cudaMemcpyHostToDevice, s->stream));
+    CK(s, cudaEventRecord(s->ev0, s->stream));
+
+    const int64_t nlaunch = (n + spl - 1) / spl;
+    const bool graph = s->use_graphs && nlaunch > 1;
+    const int v_sel0 = s->v_sel;
+    cudaGraphExec_t exec = nullptr;
+    if (graph) {
+        const std::string key = std::to_string(n) + ":" +
+                                std::to_string(spl) + ":" +
+                                std::to_string(v_sel0);
+        auto it = s->graphs.find(key);
+        if (it != s->graphs.end()) exec = it->second;
+        else {
+            CK(s, cudaStreamBeginCapture(s->stream,
+                                         cudaStreamCaptureModeThreadLocal));
         }
-        CK(s, cudaLaunchKernelExC(&lc, (const void *)s->kernel, args));
-        s->last_launches++;
-        s->n_launches++;
-        CK(s, cudaMemcpyAsync(s->h_status, s->d_status, sizeof(mkg_status),
-                              cudaMemcpyDeviceToHost, s->stream));
-        CK(s, cudaStreamSynchronize(s->stream));
-        if (s->h_status->error != MKG_DEV_OK) {
-            s->running = false;
-            return set_err(s, MKG_ERR_TIMEOUT,
-                           "device barrier wait timed out (block %d)",
-                           s->h_status->timeout_block);
-        }
-        int64_t executed = m;
-        if (s->h_status->halt_step != MKG_NO_HALT) {
-            executed = (int64_t)s->h_status->halt_step + 1;
-            halted = true;
-        }
-        s->v_sel ^= (int)(executed & 1);
-        if (!diffusion_on(s)) s->v_sel = 0;
-        done += executed;
-        s->last_cell_steps += executed * s->ncell;
-        if (halted) break;
     }
+    if (!exec) {
+        int epoch = 0;
+        for (int64_t off = 0; off < n; off += spl) {
+            const int64_t m = std::min<int64_t>(n - off, spl);
+            a.steps = s->d_steps + off;
+            a.nsteps = (int)m;
+            a.step0 = (int)off;
+            a.epoch_base = epoch;
+            a.v_sel = diffusion_on(s) ? (v_sel0 ^ (int)(off & 1)) : 0;
+            void *args[] = {&a};
+            cudaLaunchConfig_t lc;
+            memset(&lc, 0, sizeof(lc));
+            cudaLaunchAttribute attr[1];
+            lc.blockDim = dim3(bx, by, 1);
+            lc.stream = s->stream;
+            long long grid;
+            if (m > 1) {
+                grid = coop_blocks;
+                attr[0].id = cudaLaunchAttributeCooperative;
+                attr[0].val.cooperative = 1;
+                lc.attrs = attr;
+                lc.numAttrs = 1;
+                epoch += (int)(m - 1);
+            } else {
+                grid = std::min<long long>(ntiles, 1 << 30);
+            }
+            size_t smem = 0;
+            staging(grid, &a.stage_tiles, &smem);
+            lc.gridDim = dim3((unsigned)grid, 1, 1);
+            lc.dynamicSmemBytes = smem;
+            const cudaError_t e = cudaLaunchKernelExC(
+                &lc, (const void *)s->kernel, args);
+            if (e != cudaSuccess) {
+                if (graph) {
+                    cudaGraph_t g = nullptr;
+                    cudaStreamEndCapture(s->stream, &g);
+                    if (g) cudaGraphDestroy(g);
+                }
+                s->running = false;
+                return set_err(s, MKG_ERR_CUDA,
+                               "kernel launch failed: %s",
+                               cudaGetErrorString(e));
+            }
+        }
+        if (graph) {
+            cudaGraph_t g = nullptr;
+            CK(s, cudaStreamEndCapture(s->stream, &g));
+            const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess)
+                return set_err(s, MKG_ERR_CUDA, "graph instantiation: %s",
+                               cudaGetErrorString(e));
+            s->graphs[std::to_string(n) + ":" + std::to_string(spl) + ":" +
+                      std::to_string(v_sel0)] = exec;
+        }
+    }
+    if (graph) CK(s, cudaGraphLaunch(exec, s->stream));
+    s->last_launches += nlaunch;
+    s->n_launches += nlaunch;
     CK(s, cudaEventRecord(s->ev1, s->stream));
+    CK(s, cudaMemcpyAsync(s->h_status, s->d_status, sizeof(mkg_status),
+                          cudaMemcpyDeviceToHost, s->stream));
+    CK(s, cudaStreamSynchronize(s->stream));
+    if (s->h_status->error != MKG_DEV_OK) {
+        s->running = false;
+        return set_err(s, MKG_ERR_TIMEOUT,
+                       "device barrier wait timed out (block %d)",
+                       s->h_status->timeout_block);
+    }
+    int64_t done = n;
+    bool halted = false;
+    if (s->h_status->halt_step != MKG_NO_HALT) {
+        done = (int64_t)s->h_status->halt_step + 1;
+        halted = true;
+    }
+    if (diffusion_on(s)) s->v_sel = v_sel0 ^ (int)(done & 1);
+    s->last_cell_steps = done * s->ncell;
 
     /* Rows written by the executed steps */
     int64_t rows_done = 0;
@@ -1145,6 +1328,10 @@ extern "C" int mkg_set_state_static(mkg_sim *s, const double *state,
     if (n != s->ncell * s->cfg.n_state)
         return set_err(s, MKG_ERR_ARG,
                        "'state_in' must have size nx * ny * n_states.");
+    if (s->cfg.hi_mode != MKG_HI_NONE)
+        return set_err(s, MKG_ERR_ARG,
+                       "mkg_set_state_static: not available for simulations"
+                       " with accumulated states; use mkg_set_state");
     if (n > MKG_STATIC_STAGE_DOUBLES)
         return set_err(s, MKG_ERR_ARG,
                        "mkg_set_state_static: a state of %lld values exceeds"

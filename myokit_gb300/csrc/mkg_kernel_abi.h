@@ -62,6 +62,23 @@ typedef struct mkg_launch {
     int n_log_items;
     int nan_check;           /* apply the NaN halt at log rows */
     int ntiles_x, ntiles_y;  /* tiles covering the grid (2D) or cells (1D) */
+    int stage_tiles;         /* 2D: tiles whose V halo tiles are staged in
+                                shared memory per __syncthreads (the
+                                dynamic shared memory holds this many) */
+    int step0;               /* index of this launch's first step within
+                                the chunk (for the NaN halt) */
+    int epoch_base;          /* grid barriers completed by earlier launches
+                                of this chunk (the barrier counter is reset
+                                once per chunk) */
+    int pad1;
+    void *hi;                /* accumulation planes [n_hi][pitch], 8 bytes
+                                per entry: FP64 states, or FP32 Kahan
+                                compensation terms */
 } mkg_launch;
+
+/* Accumulation modes for selected states of a single precision kernel */
+#define MKG_HI_NONE   0
+#define MKG_HI_DOUBLE 1   /* state stored and updated in FP64 */
+#define MKG_HI_KAHAN  2   /* FP32 state plus FP32 compensation term */
 
 #endif /* MKG_KERNEL_ABI_H */

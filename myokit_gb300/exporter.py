@@ -73,10 +73,26 @@ class CudaExpressionWriter(CBasedExpressionWriter):
     counterpart of OpenCL's ``native_*`` functions
     (``myokit/formats/opencl/_ewriter.py:59-93``).
     """
-    def __init__(self, single, native_math=False):
+    def __init__(self, single, native_math=False, fast_divide=False):
         super().__init__()
         self._single = bool(single)
         self._native = bool(native_math) and self._single
+        self._fast_div = bool(fast_divide) and self._single
+        self.int_powers = set()
+
+    def _ex_divide(self, e):
+        if not self._fast_div:
+            return super()._ex_divide(e)
+        # Single precision fast division: a constant denominator becomes a
+        # multiplication by its rounded reciprocal (within 1.5 ulp of the
+        # quotient), any other one uses the 2-ulp hardware reciprocal.
+        num = self.ex(e[0])
+        if isinstance(e[1], myokit.Number):
+            d = float(e[1].eval())
+            if d != 0 and np.isfinite(d):
+                r = _fmt_number(float(np.float32(1.0) / np.float32(d)), True)
+                return f'(({num}) * {r})'
+        return f'__fdividef({num}, {self.ex(e[1])})'
 
     def _fn(self, name):
         if not self._single:
@@ -92,9 +108,17 @@ class CudaExpressionWriter(CBasedExpressionWriter):
     def _ex_power(self, e):
         base, exponent = e[0], e[1]
         if isinstance(exponent, myokit.Number):
-            p = exponent.eval()
-            if p in (2.0, 3.0, 4.0):
+            p = float(exponent.eval())
+            # Small integer powers by repeated squaring (the exporter emits
+            # mkg_pow<n> helpers), half-integer powers through sqrt.
+            if p == int(p) and 2 <= p <= 16:
+                self.int_powers.add(int(p))
                 return f'mkg_pow{int(p)}({self.ex(base)})'
+            if p == 0.5:
+                return self._ex_function(myokit.Sqrt(base), self._fn('sqrt'))
+            if p == 1.5:
+                b = self.ex(base)
+                return f'mkg_pow1p5({b})'
         return f'{self._fn("pow")}({self.ex(base)}, {self.ex(exponent)})'
 
     def _ex_sqrt(self, e):
@@ -168,8 +192,12 @@ class OpCensus(object):
                 self.divide += 1
             elif isinstance(x, myokit.Power):
                 p = x[1].eval() if isinstance(x[1], myokit.Number) else None
-                if p in (2.0, 3.0, 4.0):
-                    self.arith += int(p) - 1
+                if p is not None and p == int(p) and 2 <= p <= 16:
+                    self.arith += int(p).bit_length() + bin(int(p)).count(
+                        '1') - 2
+                elif p in (0.5, 1.5):
+                    self.trans += 1
+                    self.arith += 1 if p == 1.5 else 0
                 else:
                     self.power += 1
             elif isinstance(x, self._TRANS):
@@ -201,6 +229,32 @@ _LOG_BLOCK = '''
                 lg[c] = val;
             }}
         }}'''
+
+
+def _pow_helpers(single):
+    """Inline helpers for x^n (n = 2..16, by repeated squaring) and x^1.5."""
+    out = []
+    for n in range(2, 17):
+        lines = []
+        # binary exponentiation, most significant bit first
+        bits = bin(n)[3:]
+        cur = 'x'
+        k = 0
+        for b in bits:
+            lines.append(f'    const Real s{k} = {cur} * {cur};')
+            cur = f's{k}'
+            k += 1
+            if b == '1':
+                lines.append(f'    const Real s{k} = {cur} * x;')
+                cur = f's{k}'
+                k += 1
+        out.append(
+            f'static __device__ __forceinline__ Real mkg_pow{n}(Real x)\n'
+            '{\n' + '\n'.join(lines) + f'\n    return {cur};\n}}')
+    sq = 'sqrtf' if single else 'sqrt'
+    out.append('static __device__ __forceinline__ Real mkg_pow1p5(Real x)'
+               f' {{ return x * {sq}(x); }}')
+    return '\n'.join(out)
 
 
 def _read(name):
@@ -239,10 +293,16 @@ class TissueKernel(object):
     ``fast_divide``
         Single precision only: use the 2-ulp division of the hardware,
         within the 2.5 ulp that OpenCL allows for ``x / y`` by default.
+    ``math``
+        Single precision only: ``'default'`` (the above), ``'ieee'``
+        (correctly rounded division), or ``'fast'`` (reciprocal
+        multiplication for constant denominators, the hardware reciprocal
+        elsewhere, denormals flushed to zero).
     """
     def __init__(self, model, precision, native_math, bound_variables,
                  inter_log, diffusion, two_d, fields, rl_states, block,
-                 fast_divide=True, min_blocks=1):
+                 fast_divide=True, min_blocks=1, math='default',
+                 accumulate=None, accumulate_states=()):
         self.model = model
         self.single = (precision == myokit.SINGLE_PRECISION)
         self.native_math = bool(native_math)
@@ -253,7 +313,11 @@ class TissueKernel(object):
         self.fields = list(fields)
         self.rl_states = dict(rl_states)
         self.block = (int(block[0]), int(block[1]))
-        self.fast_divide = bool(fast_divide) and self.single
+        self.math = str(math) if self.single else 'ieee'
+        if self.math not in ('default', 'ieee', 'fast'):
+            raise ValueError('math must be default, ieee or fast')
+        self.fast_divide = (bool(fast_divide) and self.single
+                            and self.math != 'ieee')
         self.min_blocks = int(min_blocks)
         self.states = list(model.states())
         self.n_state = len(self.states)
@@ -262,6 +326,20 @@ class TissueKernel(object):
             self.i_vm = self.vm.index()
         else:
             self.i_vm = -1
+        # States accumulated in FP64 or with a Kahan-compensated FP32 update
+        # (single precision only; Rush-Larsen gates never need it)
+        if accumulate not in (None, 'double', 'kahan'):
+            raise ValueError('accumulate must be None, "double" or "kahan"')
+        self.accumulate = accumulate if self.single else None
+        self.hi_states = []
+        if self.accumulate:
+            chosen = set(accumulate_states)
+            for i, st in enumerate(self.states):
+                if st in chosen and st not in self.rl_states:
+                    self.hi_states.append(i)
+        self.hi_index = {i: j for j, i in enumerate(self.hi_states)}
+        self.v_double = (self.accumulate == 'double' and
+                         self.i_vm in self.hi_index)
         self.census = OpCensus()
         self._source = self._generate()
 
@@ -288,7 +366,8 @@ class TissueKernel(object):
 
     def _generate(self):
         m = self.model
-        w = CudaExpressionWriter(self.single, self.native_math)
+        w = CudaExpressionWriter(self.single, self.native_math,
+                                 self.math == 'fast')
         w.set_lhs_function(self._name)
         real = 'float' if self.single else 'double'
         prec = myokit.SINGLE_PRECISION if self.single else \
@@ -365,16 +444,29 @@ class TissueKernel(object):
 
         # State loads, and the update of each state, emitted as soon as its
         # inputs exist so that derivatives do not stay live to the end.
+        # States in self.hi_states live in the accumulation planes (hi):
+        # FP64 values ('double') or FP32 compensation terms ('kahan'; the
+        # state is x - c, updated with Kahan's compensated sum).
         loads = []
         updates = []
+        hiD = '((double *)hi)'
+        hiR = '((Real *)hi)'
         for i, s in enumerate(self.states):
             n = self._name(s)
+            j = self.hi_index.get(i)
+            plane = f'(long long){i} * pitch + cid'
+            if j is not None:
+                hplane = f'(long long){j} * pitch + cid'
             if i == self.i_vm:
-                loads.append(f'{tab}const Real {n} = V_;')
+                loads.append(f'{tab}const Real {n} = (Real)V_;')
+            elif j is not None and self.accumulate == 'double':
+                loads.append(f'{tab}const double X{n} = {hiD}[{hplane}];')
+                loads.append(f'{tab}const Real {n} = (Real)X{n};')
             else:
-                loads.append(
-                    f'{tab}const Real {n} = state[(long long){i} * pitch'
-                    f' + cid];')
+                loads.append(f'{tab}const Real {n} = state[{plane}];')
+            if j is not None and self.accumulate == 'kahan':
+                loads.append(f'{tab}const Real C{n} = {hiR}[{hplane}];')
+            target = 'vout[cid]' if i == self.i_vm else f'state[{plane}]'
             if s in self.rl_states:
                 inf, tau = self.rl_states[s]
                 need = set(
@@ -383,16 +475,26 @@ class TissueKernel(object):
                 inf, tau = ref(inf), ref(tau)
                 expf = w._fn('exp')
                 upd = f'{inf} - ({inf} - {n}) * {expf}(-dt_ / {tau})'
+                text = f'{tab}{target} = {upd};'
                 self.census.arith += 4
                 self.census.trans += 1
             else:
-                need = set([self._name(s.lhs())])
-                upd = f'{n} + dt_ * {self._name(s.lhs())}'
+                d = self._name(s.lhs())
+                need = set([d])
                 self.census.arith += 2
-            if i == self.i_vm:
-                text = f'{tab}vout[cid] = {upd};'
-            else:
-                text = f'{tab}state[(long long){i} * pitch + cid] = {upd};'
+                if j is None:
+                    text = f'{tab}{target} = {n} + dt_ * {d};'
+                elif self.accumulate == 'double':
+                    cur = 'V_' if i == self.i_vm else f'X{n}'
+                    dst = target if i == self.i_vm else f'{hiD}[{hplane}]'
+                    text = f'{tab}{dst} = {cur} + (double)(dt_ * {d});'
+                else:
+                    text = (
+                        f'{tab}{{ const Real y_ = dt_ * {d} - C{n};\n'
+                        f'{tab}  const Real s_ = {n} + y_;\n'
+                        f'{tab}  {hiR}[{hplane}] = (s_ - {n}) - y_;\n'
+                        f'{tab}  {target} = s_; }}')
+                    self.census.arith += 3
             updates.append((i, need, text))
 
         defined = set(self._name(v) for v in self.fields)
@@ -441,7 +543,7 @@ class TissueKernel(object):
         first = self._name(self.states[0])
         log_a += (
             f'\n{tab}if (row >= 0 && a.nan_check && cid == 0 && '
-            f'isnan({first}))\n{tab}    atomicMin(&a.status->halt_step, k);')
+            f'isnan({first}))\n{tab}    atomicMin(&a.status->halt_step, a.step0 + k);')
         log_b = ''
         if self.inter_log:
             cases = [f'case {self.n_state + 1 + k}: val = {name}; break;'
@@ -452,6 +554,7 @@ class TissueKernel(object):
 
         subs = {
             '@REAL@': real,
+            '@VREAL@': 'double' if self.v_double else real,
             '@SINGLE@': '1' if self.single else '0',
             '@N_STATE@': str(self.n_state),
             '@N_FIELD@': str(len(self.fields)),
@@ -462,6 +565,7 @@ class TissueKernel(object):
             '@BX@': str(self.block[0]),
             '@BY@': str(self.block[1]),
             '@MINB@': str(self.min_blocks),
+            '@POW_HELPERS@': _pow_helpers(self.single),
             '@LOADS@': '\n'.join(loads),
             '@LOG_A@': log_a,
             '@BODY@': '\n'.join(body),
@@ -494,7 +598,7 @@ class TissueKernel(object):
                 opts.append('--prec-div=false')
             opts.append('--prec-sqrt=false' if self.native_math else
                         '--prec-sqrt=true')
-            opts.append('--ftz=false')
+            opts.append('--ftz=true' if self.math == 'fast' else '--ftz=false')
         opts.append('--fmad=true')
         return opts
 
@@ -513,6 +617,9 @@ class TissueKernel(object):
         """
         r = 4 if self.single else 8
         b = 2 * self.n_state * r + len(self.fields) * r
+        # FP64 storage doubles a state's bytes; a Kahan term adds a Real
+        b += 2 * len(self.hi_states) * (8 - r if self.accumulate == 'double'
+                                        else r)
         if self.diffusion == DIFF_HETERO:
             b += 2 * r
         return b

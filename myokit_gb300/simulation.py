@@ -117,13 +117,29 @@ class SimulationCUDA(object):
         Time steps fused into one kernel launch (0 = a whole chunk).
     ``device``
         CUDA device ordinal.
+    ``min_blocks``
+        Minimum resident CTAs per SM asked of the compiler (caps registers).
+    ``fp32_math``
+        Single precision arithmetic: ``'default'`` (2-ulp division, as
+        OpenCL allows), ``'ieee'`` (correctly rounded division) or
+        ``'fast'`` (reciprocal multiplication, flush-to-zero).
+    ``accumulate``
+        Single precision only. ``None``: every state in FP32. ``'double'``:
+        the selected states are stored and updated in FP64 while the
+        right-hand side is evaluated in FP32. ``'kahan'``: the selected
+        states stay FP32 and are updated with a compensated (Kahan) sum.
+    ``accumulate_states``
+        The states to accumulate; by default the membrane potential, states
+        with concentration units and non-gating states of magnitude >= 1,
+        whose per-step increments are smallest relative to their value.
     """
     _index = 0
 
     def __init__(
             self, model, protocol=None, ncells=256, diffusion=True,
             precision=myokit.SINGLE_PRECISION, native_maths=False, rl=False,
-            block=None, steps_per_launch=0, device=0, min_blocks=None):
+            block=None, steps_per_launch=0, device=0, min_blocks=None,
+            fp32_math='default', accumulate=None, accumulate_states=None):
 
         # Model checks (openclsim.py:155-167)
         if not model.is_valid():
@@ -225,7 +241,29 @@ class SimulationCUDA(object):
         # GPU options
         self._block = block
         self._min_blocks = min_blocks
+        self._fp32_math = fp32_math
+        if accumulate not in (None, 'double', 'kahan'):
+            raise ValueError(
+                'The argument "accumulate" must be None, "double" or'
+                ' "kahan".')
+        if accumulate is not None and precision != myokit.SINGLE_PRECISION:
+            raise ValueError(
+                'Accumulation modes apply to single precision simulations.')
+        self._accumulate = accumulate
+        self._acc_names = None
+        if accumulate_states is not None:
+            self._acc_names = [
+                v.qname() if isinstance(v, myokit.Variable) else str(v)
+                for v in accumulate_states]
+            for name in self._acc_names:
+                if not self._model.get(name).is_state():
+                    raise ValueError(
+                        'Accumulated variables must be states: ' + name)
         self._steps_per_launch = int(steps_per_launch)
+        self._blocks_per_sm = 0
+        self._graphs = 1
+        self._tune_sig = None
+        self._tune_hit = None
         self._device = int(device)
         self._backend = None
         self._last_stats = None
@@ -695,10 +733,25 @@ class SimulationCUDA(object):
             return _exp.DIFF_HETERO
         return _exp.DIFF_GRID
 
+    def _tuned_choice(self):
+        """A cached autotuner result for this configuration, or None."""
+        from . import autotune
+        sig = autotune.signature(self)
+        if self._tune_sig != sig:
+            self._tune_sig = sig
+            self._tune_hit = autotune.lookup(self)
+        return self._tune_hit
+
     def _block_shape(self, two_d):
         b = self._block
         if b is None:
-            return (32, 4) if two_d else (128, 1)
+            hit = self._tuned_choice()
+            if hit is not None:
+                b = tuple(hit['block'])
+            elif self._precision == myokit.DOUBLE_PRECISION:
+                b = (32, 4) if two_d else (128, 1)
+            else:
+                b = (64, 4) if two_d else (256, 1)
         if isinstance(b, int):
             return (b, 1) if not two_d else (32, max(1, b // 32))
         bx, by = int(b[0]), int(b[1])
@@ -711,7 +764,53 @@ class SimulationCUDA(object):
         the registers per thread at 64K / (threads * min_blocks)."""
         if self._min_blocks is not None:
             return int(self._min_blocks)
-        return 1
+        if self._block is None:
+            hit = self._tuned_choice()
+            if hit is not None:
+                return int(hit['min_blocks'])
+        if self._precision == myokit.DOUBLE_PRECISION:
+            return 1
+        # 128 registers per thread: 64K registers / 512 threads
+        return max(1, 512 // (block[0] * block[1]))
+
+    def _launch_steps(self):
+        """Steps per launch: explicit, cached by the autotuner, or 0."""
+        if self._steps_per_launch:
+            return self._steps_per_launch
+        if self._block is None:
+            hit = self._tuned_choice()
+            if hit is not None:
+                return int(hit.get('steps_per_launch', 0))
+        return 0
+
+    def autotune(self, duration=None, verbose=False):
+        """
+        Times candidate launch shapes on this simulation (state and time
+        are restored afterwards), keeps the fastest and caches it for
+        simulations with the same configuration. Returns the choice.
+        """
+        from . import autotune
+        best, results = autotune.autotune(self, duration, verbose=verbose)
+        self._tune_sig = None
+        return best
+
+    def accumulated_states(self):
+        """The states accumulated in FP64 or with a compensated update."""
+        if self._accumulate is None:
+            return []
+        if self._acc_names is not None:
+            return [self._model.get(n) for n in self._acc_names]
+        conc = myokit.parse_unit('mM').exponents()
+        out = []
+        for st in self._model.states():
+            u = st.unit()
+            if st is self._vm:
+                out.append(st)
+            elif u is not None and u.exponents() == conc:
+                out.append(st)
+            elif st not in self._rl_states and abs(st.initial_value(True)) >= 1:
+                out.append(st)
+        return out
 
     def _kernel(self, inter_log):
         """The generated kernel for the current configuration."""
@@ -723,7 +822,9 @@ class SimulationCUDA(object):
             self._model, self._precision, self._native_math,
             self._bound_variables, inter_log, mode, two_d,
             list(self._fields.keys()), self._rl_states, block,
-            min_blocks=self._default_min_blocks(block))
+            min_blocks=self._default_min_blocks(block),
+            math=self._fp32_math, accumulate=self._accumulate,
+            accumulate_states=self.accumulated_states())
 
     def _get_backend(self, kernel):
         """A host-library handle for this kernel, reused between runs."""
@@ -740,6 +841,9 @@ class SimulationCUDA(object):
         cfg.block_x, cfg.block_y = kernel.block
         cfg.device = self._device
         cfg.two_d = 1 if kernel.two_d else 0
+        cfg.hi_mode = {None: 0, 'double': 1, 'kahan': 2}[kernel.accumulate] \
+            if kernel.hi_states else 0
+        cfg.n_hi = len(kernel.hi_states)
         key = (kernel.key(), bytes(cfg))
         if self._backend is not None and self._backend[0] == key:
             return self._backend[1]
@@ -747,6 +851,9 @@ class SimulationCUDA(object):
             self._backend[1].close()
             self._backend = None
         be = _Backend(kernel, cfg)
+        if cfg.n_hi:
+            hs = np.ascontiguousarray(kernel.hi_states, dtype=np.int32)
+            be.check(be.lib.mkg_set_hi_states(be.h, _lib.i32ptr(hs), len(hs)))
         self._backend = (key, be)
         return be
 
@@ -926,7 +1033,8 @@ class SimulationCUDA(object):
         be.check(lib.mkg_set_log(
             h, _lib.i32ptr(items), _lib.i64ptr(cells), len(cols),
             1 if logging_states else 0))
-        be.check(lib.mkg_set_tuning(h, self._steps_per_launch, 0))
+        be.check(lib.mkg_set_tuning(h, self._launch_steps(),
+                                    self._blocks_per_sm, self._graphs))
         be.check(lib.mkg_run_begin(h, tmin, tmax, self._step_size,
                                    log_interval))
 

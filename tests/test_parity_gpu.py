@@ -311,3 +311,48 @@ def test_sheet2048_runs(decker):
     st = s.state_array().reshape(2048, 2048, -1)
     assert np.all(np.isfinite(st))
     assert np.array_equal(st[0], st[2047])
+
+
+# ---------------------------------------------------------------------------
+# Launch grouping and tuning change nothing in the results
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize('spl,block', [(1, None), (7, None), (0, (32, 2)),
+                                       (5, (64, 8))])
+def test_launch_grouping_is_exact(decker, spl, block):
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    out = []
+    for kw in ({}, {'steps_per_launch': spl, 'block': block}):
+        s = mg.SimulationCUDA(decker, p, ncells=(70, 33), rl=True, **kw)
+        s.set_paced_cells(3, 33)
+        d = s.run(3, log=['engine.time', '5.5.membrane.V',
+                          '69.32.membrane.V'], log_interval=0.1)
+        out.append((s.state_array(), d))
+    assert np.array_equal(out[0][0], out[1][0])
+    for k in out[0][1].keys():
+        assert np.array_equal(np.asarray(out[0][1][k]),
+                              np.asarray(out[1][1][k]))
+
+
+def test_nan_halt_across_launches():
+    import test_oracle as to
+    s = to.nan_sim(mg.SimulationCUDA)
+    s._steps_per_launch = 7
+    with pytest.raises(myokit.SimulationError, match='Time:  1.23'):
+        s.run(5)
+
+
+def test_autotune_keeps_results(br77, tmp_path, monkeypatch):
+    monkeypatch.setenv('MYOKIT_GB300_CACHE', str(tmp_path))
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    s = mg.SimulationCUDA(br77, p, ncells=(40, 40))
+    x0 = s.state_array()
+    best = s.autotune(duration=0.2)
+    assert best is not None
+    assert np.array_equal(s.state_array(), x0) and s.time() == 0
+    s.run(2)
+    a = s.state_array()
+    c = mg.SimulationCUDA(br77, p, ncells=(40, 40))   # picks the cache
+    assert c._tuned_choice() is not None
+    c.run(2)
+    assert np.array_equal(a, c.state_array())
