@@ -43,8 +43,7 @@ METRIC = 'cell-steps/s on 1 GB300 (FP32 vs FP64 at stated max|dV|)'
 VARIANTS = [
     ('fp32+double', {'accumulate': 'double'}),
     ('fp32+kahan', {'accumulate': 'kahan'}),
-    ('fp32-fast', {'fp32_math': 'fast'}),
-    ('fp32-fast+kahan', {'fp32_math': 'fast', 'accumulate': 'kahan'}),
+    ('fp32-ieee-div', {'fp32_math': 'ieee'}),
 ]
 UNIT = 'cell-steps/s'
 

@@ -1,9 +1,8 @@
 """
 Launch-shape autotuner for :class:`SimulationCUDA`.
 
-The fused kernel's speed depends on the CTA shape (which sets the tile of
-cells that shares one shared-memory V halo), on the register cap that the
-minimum number of resident CTAs per SM implies, and on how steps are
+The fused kernel's speed depends on the CTA size, on the register cap that
+the minimum number of resident CTAs per SM implies, and on how steps are
 grouped into launches (one cooperative launch per chunk with a grid barrier
 between steps, or one plain launch per step replayed from a CUDA graph).
 :func:`autotune` times candidates on the simulation itself -- same model,
@@ -19,15 +18,13 @@ import numpy as np
 
 from ._deps import myokit
 
-# Candidate (block, min CTAs per SM, steps per launch)
-_CANDIDATES_2D = [
-    ((64, 4), 2, 0), ((32, 8), 2, 0), ((32, 4), 4, 0), ((32, 4), 1, 0),
-    ((64, 2), 4, 0), ((32, 6), 3, 0), ((64, 4), 2, 1), ((32, 4), 4, 1),
+# Candidate (threads per CTA, min CTAs per SM, steps per launch); the
+# register cap is 64K / (threads * min CTAs)
+_CANDIDATES = [
+    ((256, 1), 2, 0), ((128, 1), 4, 0), ((512, 1), 1, 0), ((192, 1), 3, 0),
+    ((384, 1), 1, 0), ((128, 1), 1, 0), ((256, 1), 2, 1), ((128, 1), 4, 1),
 ]
-_CANDIDATES_1D = [
-    ((256, 1), 2, 0), ((128, 1), 4, 0), ((128, 1), 1, 0), ((192, 1), 3, 0),
-    ((64, 1), 8, 0), ((256, 1), 2, 1), ((128, 1), 4, 1),
-]
+_CANDIDATES_FP64 = [((128, 1), 1, 0), ((256, 1), 1, 0), ((64, 1), 1, 0)]
 
 
 def _cache_path():
@@ -85,14 +82,10 @@ def autotune(sim, duration=None, candidates=None, store=True,
     returns ``(best, results)``. ``results`` maps each candidate to its
     cell-steps per second of device time.
     """
-    two_d = len(sim._dims) == 2 and sim._diffusion_enabled and \
-        sim._connections is None
     if candidates is None:
-        candidates = _CANDIDATES_2D if two_d else _CANDIDATES_1D
-        if sim._precision == myokit.DOUBLE_PRECISION:
-            # FP64 kernels spill when registers are capped
-            candidates = [c for c in candidates if c[1] == 1] or [
-                ((32, 4) if two_d else (128, 1), 1, 0)]
+        # FP64 kernels spill when registers are capped
+        candidates = _CANDIDATES_FP64 \
+            if sim._precision == myokit.DOUBLE_PRECISION else _CANDIDATES
     if duration is None:
         steps = max(20, int(4e8 / sim._ntotal))
         if sim._precision == myokit.DOUBLE_PRECISION:

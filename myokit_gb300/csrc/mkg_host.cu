@@ -35,9 +35,6 @@
 #include "mkg_kernel_abi.h"
 #include "mkg_pacing.h"
 
-/* Shared memory per CTA for staged V tiles (2D kernels) */
-#define MKG_STAGE_BUDGET 24576
-
 namespace {
 
 thread_local std::string g_thread_error;
@@ -156,7 +153,6 @@ struct mkg_sim {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t kernel = nullptr;
     int occ_blocks = 1;       /* co-resident blocks per SM */
-    int stage_budget = 0;     /* dynamic shared memory per CTA (bytes) */
     int num_sms = 1;
 
     /* device buffers */
@@ -513,8 +509,9 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
     if (cfg->block_x < 1 || cfg->block_y < 1 ||
         cfg->block_x * cfg->block_y > 1024)
         return set_err(nullptr, MKG_ERR_ARG, "invalid block shape");
-    if (!cfg->two_d && cfg->block_y != 1)
-        return set_err(nullptr, MKG_ERR_ARG, "flat kernels need block_y 1");
+    if (cfg->block_y != 1 || cfg->block_x % 32 != 0)
+        return set_err(nullptr, MKG_ERR_ARG,
+                       "the CTA must be (32*k, 1) threads");
     if (!cfg->two_d && cfg->ny != 1 && cfg->diffusion != MKG_DIFF_NONE)
         return set_err(nullptr, MKG_ERR_ARG, "2D diffusion needs two_d");
 
@@ -544,12 +541,9 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
     CKC(cudaLibraryGetKernel(&s->kernel, s->lib, "mkg_tissue_step"));
     CKC(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount,
                                cfg->device));
-    /* 2D kernels stage V tiles in dynamic shared memory, at most
-     * MKG_STAGE_BUDGET bytes per CTA; occupancy is computed for that. */
-    s->stage_budget = cfg->two_d ? MKG_STAGE_BUDGET : 0;
     CKC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &s->occ_blocks, (const void *)s->kernel,
-        cfg->block_x * cfg->block_y, s->stage_budget));
+        cfg->block_x * cfg->block_y, 0));
     if (s->occ_blocks < 1) {
         set_err(nullptr, MKG_ERR_CUDA,
                 "the generated kernel cannot be resident on an SM");
@@ -985,36 +979,25 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
     a.status = s->d_status;
     a.timeout_ns = s->timeout_ns;
     a.hi = s->d_hi;
+    /* Warp tiles: 32 consecutive cells of a row (2D) or of the flat cell
+     * array (1D cables, connection graphs, diffusion-free simulations). */
     if (two_d) {
-        a.ntiles_x = (int)((s->cfg.nx + bx - 1) / bx);
-        a.ntiles_y = (int)((s->cfg.ny + by - 1) / by);
+        a.ntiles_x = (int)((s->cfg.nx + 31) / 32);
+        a.ntiles_y = (int)s->cfg.ny;
     } else {
-        /* Flat cell array: 1D cables, connection graphs and diffusion-free
-         * simulations (whose cells are independent). */
         a.nx = s->ncell;
         a.ny = 1;
-        a.ntiles_x = (int)((s->ncell + bx - 1) / bx);
+        a.ntiles_x = (int)((s->ncell + 31) / 32);
         a.ntiles_y = 1;
     }
-    const long long ntiles = (long long)a.ntiles_x * a.ntiles_y;
+    a.stage_tiles = 0;
+    const int threads = bx * by;
+    const long long nwt = (long long)a.ntiles_x * a.ntiles_y;
+    const long long blocks_needed = (nwt * 32 + threads - 1) / threads;
     int bpsm = s->blocks_per_sm > 0 ? std::min(s->blocks_per_sm, s->occ_blocks)
                                     : s->occ_blocks;
-    long long coop_blocks = std::min<long long>(ntiles,
+    long long coop_blocks = std::min<long long>(blocks_needed,
                                                 (long long)bpsm * s->num_sms);
-    /* Tiles staged per __syncthreads and the shared memory that takes */
-    const size_t tile_bytes = (size_t)(bx + 2) * (by + 2) * s->vbytes;
-    auto staging = [&](long long grid, int *stage_tiles, size_t *smem) {
-        const long long per = (ntiles + grid - 1) / grid;
-        if (!two_d) {
-            *stage_tiles = (int)std::min<long long>(per, INT_MAX);
-            *smem = 0;
-            return;
-        }
-        long long m = std::max<long long>(
-            1, std::min<long long>(per, s->stage_budget / tile_bytes));
-        *stage_tiles = (int)m;
-        *smem = (size_t)m * tile_bytes;
-    };
     int spl = s->steps_per_launch > 0 ? s->steps_per_launch : 1 << 20;
 
     /* All launches of the chunk are queued without host synchronisation;
@@ -1059,7 +1042,7 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
             cudaLaunchConfig_t lc;
             memset(&lc, 0, sizeof(lc));
             cudaLaunchAttribute attr[1];
-            lc.blockDim = dim3(bx, by, 1);
+            lc.blockDim = dim3(threads, 1, 1);
             lc.stream = s->stream;
             long long grid;
             if (m > 1) {
@@ -1070,12 +1053,10 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
                 lc.numAttrs = 1;
                 epoch += (int)(m - 1);
             } else {
-                grid = std::min<long long>(ntiles, 1 << 30);
+                grid = std::min<long long>(blocks_needed, 1 << 30);
             }
-            size_t smem = 0;
-            staging(grid, &a.stage_tiles, &smem);
             lc.gridDim = dim3((unsigned)grid, 1, 1);
-            lc.dynamicSmemBytes = smem;
+            lc.dynamicSmemBytes = 0;
             const cudaError_t e = cudaLaunchKernelExC(
                 &lc, (const void *)s->kernel, args);
             if (e != cudaSuccess) {

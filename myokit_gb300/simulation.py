@@ -120,9 +120,12 @@ class SimulationCUDA(object):
     ``min_blocks``
         Minimum resident CTAs per SM asked of the compiler (caps registers).
     ``fp32_math``
-        Single precision arithmetic: ``'default'`` (2-ulp division, as
-        OpenCL allows), ``'ieee'`` (correctly rounded division) or
-        ``'fast'`` (reciprocal multiplication, flush-to-zero).
+        Single precision arithmetic. ``'fast'`` (the default): a division by
+        a constant becomes a multiplication by its reciprocal (1.5 ulp),
+        other divisions use the 2-ulp hardware reciprocal, denormals flush
+        to zero -- all within what OpenCL allows single precision by
+        default. ``'default'``: the compiler's 2-ulp division, denormals
+        kept. ``'ieee'``: correctly rounded division.
     ``accumulate``
         Single precision only. ``None``: every state in FP32. ``'double'``:
         the selected states are stored and updated in FP64 while the
@@ -139,7 +142,7 @@ class SimulationCUDA(object):
             self, model, protocol=None, ncells=256, diffusion=True,
             precision=myokit.SINGLE_PRECISION, native_maths=False, rl=False,
             block=None, steps_per_launch=0, device=0, min_blocks=None,
-            fp32_math='default', accumulate=None, accumulate_states=None):
+            fp32_math='fast', accumulate=None, accumulate_states=None):
 
         # Model checks (openclsim.py:155-167)
         if not model.is_valid():
@@ -743,21 +746,20 @@ class SimulationCUDA(object):
         return self._tune_hit
 
     def _block_shape(self, two_d):
+        """CTA shape (threads, 1); threads is a multiple of the warp size."""
         b = self._block
         if b is None:
             hit = self._tuned_choice()
             if hit is not None:
                 b = tuple(hit['block'])
             elif self._precision == myokit.DOUBLE_PRECISION:
-                b = (32, 4) if two_d else (128, 1)
+                b = 128
             else:
-                b = (64, 4) if two_d else (256, 1)
-        if isinstance(b, int):
-            return (b, 1) if not two_d else (32, max(1, b // 32))
-        bx, by = int(b[0]), int(b[1])
-        if not two_d:
-            return (bx * by, 1)
-        return (bx, by)
+                b = 256
+        if not isinstance(b, int):
+            b = int(np.prod([int(x) for x in b]))
+        b = max(32, (int(b) + 31) // 32 * 32)
+        return (min(b, 1024), 1)
 
     def _default_min_blocks(self, block):
         """Minimum resident CTAs per SM asked of the compiler, which caps
