@@ -219,6 +219,29 @@ int mkg_set_tuning(mkg_sim *sim, int32_t steps_per_launch,
 int mkg_last_stats(const mkg_sim *sim, double *kernel_ms, int64_t *launches,
                    int64_t *cell_steps);
 
+/*
+ * Discrete adjoint (no counterpart in the reference, which has no
+ * derivatives of its simulations). For a loss on logged V values it gives
+ * the exact gradients of the discrete forward map with respect to the
+ * scalar fields and to gx, gy.
+ *
+ * mkg_adj_attach loads the module generated by myokit_gb300.adjoint (the
+ * forward kernel with trajectory output and the reverse kernel) and sets
+ * the checkpoint segment length. mkg_adj_forward runs [tmin, tmax) like
+ * mkg_run_begin + mkg_run_chunk, keeping a checkpoint every seg_steps steps
+ * and all log rows (mkg_adj_read_log, rows x ncol). mkg_adj_backward takes
+ * dL/d(log value) (rows x ncol; every column must log V) and writes the
+ * field gradients (AoS, ncell x n_field) and dL/dgx, dL/dgy. Homogeneous
+ * grid diffusion or none; no accumulation modes.
+ */
+int mkg_adj_attach(mkg_sim *sim, const void *cubin, size_t size,
+                   int32_t seg_steps);
+int mkg_adj_forward(mkg_sim *sim, double tmin, double tmax, double dt,
+                    double log_interval, int64_t *rows);
+int mkg_adj_read_log(mkg_sim *sim, double *values, int64_t rows);
+int mkg_adj_backward(mkg_sim *sim, const double *lgrad, int64_t rows,
+                     double *grad_fields, double *grad_g);
+
 /* The cudaStream_t (as void*) all work of this handle is queued on, so a
  * caller can time it with events recorded on the same stream. */
 int mkg_stream(const mkg_sim *sim, void **stream);

@@ -108,6 +108,16 @@ SIGNATURES = {
     'mkg_last_stats': (ctypes.c_int, [
         ctypes.c_void_p, _c_double_p, _c_int64_p, _c_int64_p]),
     'mkg_launch_count': (ctypes.c_int, [ctypes.c_void_p, _c_int64_p]),
+    'mkg_adj_attach': (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int32]),
+    'mkg_adj_forward': (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+        ctypes.c_double, _c_int64_p]),
+    'mkg_adj_read_log': (ctypes.c_int, [
+        ctypes.c_void_p, _c_double_p, ctypes.c_int64]),
+    'mkg_adj_backward': (ctypes.c_int, [
+        ctypes.c_void_p, _c_double_p, ctypes.c_int64, _c_double_p,
+        _c_double_p]),
     'mkg_stream': (ctypes.c_int, [
         ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     'mkg_schedule_preview': (ctypes.c_int64, [

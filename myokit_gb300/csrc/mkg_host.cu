@@ -205,6 +205,26 @@ struct mkg_sim {
     int64_t n_launches = 0;   /* every kernel launched by this handle */
     bool use_graphs = false;  /* replay multi-launch chunks as CUDA graphs */
     std::map<std::string, cudaGraphExec_t> graphs;
+
+    /* Logged columns (host copy) */
+    std::vector<int> h_log_item;
+    std::vector<long long> h_log_cell;
+
+    /* Adjoint */
+    cudaLibrary_t adj_lib = nullptr;
+    cudaKernel_t adj_fwd = nullptr, adj_bwd = nullptr;
+    int adj_occ_fwd = 1, adj_occ_bwd = 1;
+    int adj_seg = 0;                      /* steps per checkpoint segment */
+    void *d_traj = nullptr, *d_lam = nullptr, *d_mu = nullptr;
+    void *d_gfield = nullptr, *d_gg = nullptr, *d_lgrad = nullptr;
+    int *d_probe_col = nullptr;
+    mkg_step *d_fsteps = nullptr, *d_bsteps = nullptr;
+    std::vector<mkg_step> adj_sched;      /* full run, global log rows */
+    std::vector<long long> adj_seg_start, adj_seg_len;
+    std::vector<int> adj_seg_vsel;
+    std::vector<void *> adj_ckpt;         /* state + V plane per segment */
+    std::vector<double> adj_log;          /* rows x log_ncol */
+    int64_t adj_rows = 0;
 };
 
 namespace {
@@ -383,6 +403,61 @@ int pacer_err(mkg_sim *s, int st)
                    st);
 }
 
+/* The launch block common to every tissue-step launch of a handle:
+ * buffers, geometry (warp tiles), conductances, pacing, logging. */
+void fill_launch(mkg_sim *s, mkg_launch *a)
+{
+    memset(a, 0, sizeof(*a));
+    a->nx = s->cfg.nx;
+    a->ny = s->cfg.ny;
+    a->ncell = s->ncell;
+    a->pitch = s->pitch;
+    a->state = s->d_state;
+    a->vbuf = s->d_vbuf;
+    a->field = s->d_field;
+    a->gx = s->d_gx;
+    a->gy = s->d_gy;
+    a->nbr_ptr = s->d_nbr_ptr;
+    a->nbr_idx = s->d_nbr_idx;
+    a->nbr_g = s->d_nbr_g;
+    a->gxs = s->gx;
+    a->gys = s->gy;
+    a->pace_x0 = s->px0;
+    a->pace_x1 = s->px1;
+    a->pace_y0 = s->py0;
+    a->pace_y1 = s->py1;
+    a->pace_bits = s->d_pace_bits;
+    a->pace_mode = s->pace_mode;
+    a->log = s->d_log;
+    a->log_items = s->d_log_items;
+    a->log_cols = s->d_log_cols;
+    a->log_ncol = s->log_ncol;
+    a->n_log_items = s->n_log_items;
+    a->nan_check = s->nan_check;
+    a->status = s->d_status;
+    a->timeout_ns = s->timeout_ns;
+    a->hi = s->d_hi;
+    /* Warp tiles: 32 consecutive cells of a row (2D) or of the flat cell
+     * array (1D cables, connection graphs, diffusion-free simulations). */
+    if (s->cfg.two_d) {
+        a->ntiles_x = (int)((s->cfg.nx + 31) / 32);
+        a->ntiles_y = (int)s->cfg.ny;
+    } else {
+        a->nx = s->ncell;
+        a->ny = 1;
+        a->ntiles_x = (int)((s->ncell + 31) / 32);
+        a->ntiles_y = 1;
+    }
+}
+
+/* CTAs needed to give every warp tile a warp */
+long long blocks_needed(const mkg_sim *s, const mkg_launch *a)
+{
+    const long long nwt = (long long)a->ntiles_x * a->ntiles_y;
+    const int threads = s->cfg.block_x * s->cfg.block_y;
+    return (nwt * 32 + threads - 1) / threads;
+}
+
 }  // namespace
 
 /* ------------------------------------------------------------------------ */
@@ -453,6 +528,18 @@ void mkg_destroy(mkg_sim *s)
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
     clear_graphs(s);
+    for (void *p : s->adj_ckpt) cudaFree(p);
+    s->adj_ckpt.clear();
+    dfree(s->d_traj);
+    dfree(s->d_lam);
+    dfree(s->d_mu);
+    dfree(s->d_gfield);
+    dfree(s->d_gg);
+    dfree(s->d_lgrad);
+    dfree(s->d_probe_col);
+    dfree(s->d_fsteps);
+    dfree(s->d_bsteps);
+    if (s->adj_lib) cudaLibraryUnload(s->adj_lib);
     dfree(s->d_state);
     dfree(s->d_vbuf);
     dfree(s->d_field);
@@ -831,6 +918,8 @@ int mkg_set_log(mkg_sim *s, const int32_t *item, const int64_t *cell,
                           s->stream));
     CK(s, cudaStreamSynchronize(s->stream));
     s->n_log_items = (int)items.size();
+    s->h_log_item.assign(item, item + ncol);
+    s->h_log_cell.assign(cell, cell + ncol);
     /* A new column count invalidates the log buffers. */
     if ((int)ncol != s->log_ncol) {
         dfree(s->d_log);
@@ -947,56 +1036,13 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
 
     /* Launch geometry */
     const int bx = s->cfg.block_x, by = s->cfg.block_y;
-    const bool two_d = s->cfg.two_d != 0;
     mkg_launch a;
-    memset(&a, 0, sizeof(a));
-    a.nx = s->cfg.nx;
-    a.ny = s->cfg.ny;
-    a.ncell = s->ncell;
-    a.pitch = s->pitch;
-    a.state = s->d_state;
-    a.vbuf = s->d_vbuf;
-    a.field = s->d_field;
-    a.gx = s->d_gx;
-    a.gy = s->d_gy;
-    a.nbr_ptr = s->d_nbr_ptr;
-    a.nbr_idx = s->d_nbr_idx;
-    a.nbr_g = s->d_nbr_g;
-    a.gxs = s->gx;
-    a.gys = s->gy;
-    a.pace_x0 = s->px0;
-    a.pace_x1 = s->px1;
-    a.pace_y0 = s->py0;
-    a.pace_y1 = s->py1;
-    a.pace_bits = s->d_pace_bits;
-    a.pace_mode = s->pace_mode;
-    a.log = s->d_log;
-    a.log_items = s->d_log_items;
-    a.log_cols = s->d_log_cols;
-    a.log_ncol = s->log_ncol;
-    a.n_log_items = s->n_log_items;
-    a.nan_check = s->nan_check;
-    a.status = s->d_status;
-    a.timeout_ns = s->timeout_ns;
-    a.hi = s->d_hi;
-    /* Warp tiles: 32 consecutive cells of a row (2D) or of the flat cell
-     * array (1D cables, connection graphs, diffusion-free simulations). */
-    if (two_d) {
-        a.ntiles_x = (int)((s->cfg.nx + 31) / 32);
-        a.ntiles_y = (int)s->cfg.ny;
-    } else {
-        a.nx = s->ncell;
-        a.ny = 1;
-        a.ntiles_x = (int)((s->ncell + 31) / 32);
-        a.ntiles_y = 1;
-    }
-    a.stage_tiles = 0;
+    fill_launch(s, &a);
     const int threads = bx * by;
-    const long long nwt = (long long)a.ntiles_x * a.ntiles_y;
-    const long long blocks_needed = (nwt * 32 + threads - 1) / threads;
+    const long long nblocks = blocks_needed(s, &a);
     int bpsm = s->blocks_per_sm > 0 ? std::min(s->blocks_per_sm, s->occ_blocks)
                                     : s->occ_blocks;
-    long long coop_blocks = std::min<long long>(blocks_needed,
+    long long coop_blocks = std::min<long long>(nblocks,
                                                 (long long)bpsm * s->num_sms);
     int spl = s->steps_per_launch > 0 ? s->steps_per_launch : 1 << 20;
 
@@ -1053,7 +1099,7 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
                 lc.numAttrs = 1;
                 epoch += (int)(m - 1);
             } else {
-                grid = std::min<long long>(blocks_needed, 1 << 30);
+                grid = std::min<long long>(nblocks, 1 << 30);
             }
             lc.gridDim = dim3((unsigned)grid, 1, 1);
             lc.dynamicSmemBytes = 0;
@@ -1324,4 +1370,309 @@ extern "C" int mkg_set_state_static(mkg_sim *s, const double *state,
     if (r) return r;
     if (s->real == 4) return upload_state_static<float>(s, state, stage);
     return upload_state_static<double>(s, state, stage);
+}
+
+
+/* ------------------------------------------------------------------------ */
+/* Discrete adjoint                                                         */
+/* ------------------------------------------------------------------------ */
+
+extern "C" int mkg_adj_attach(mkg_sim *s, const void *cubin, size_t size,
+                              int32_t seg_steps)
+{
+    if (!s || !cubin || !size) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (seg_steps < 1) return set_err(s, MKG_ERR_ARG, "seg_steps < 1");
+    if (s->cfg.hi_mode != MKG_HI_NONE)
+        return set_err(s, MKG_ERR_ARG,
+                       "the adjoint runs without accumulation modes");
+    if (s->cfg.diffusion != MKG_DIFF_NONE &&
+        s->cfg.diffusion != MKG_DIFF_GRID)
+        return set_err(s, MKG_ERR_ARG,
+                       "the adjoint supports homogeneous grid diffusion");
+    if (s->adj_lib) {
+        cudaLibraryUnload(s->adj_lib);
+        s->adj_lib = nullptr;
+    }
+    CK(s, cudaLibraryLoadData(&s->adj_lib, cubin, nullptr, nullptr, 0,
+                              nullptr, nullptr, 0));
+    CK(s, cudaLibraryGetKernel(&s->adj_fwd, s->adj_lib, "mkg_tissue_step"));
+    CK(s, cudaLibraryGetKernel(&s->adj_bwd, s->adj_lib,
+                               "mkg_tissue_adjoint"));
+    const int threads = s->cfg.block_x * s->cfg.block_y;
+    CK(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &s->adj_occ_fwd, (const void *)s->adj_fwd, threads, 0));
+    CK(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &s->adj_occ_bwd, (const void *)s->adj_bwd, threads, 0));
+    if (s->adj_occ_fwd < 1 || s->adj_occ_bwd < 1)
+        return set_err(s, MKG_ERR_CUDA, "adjoint kernels cannot be resident");
+    const size_t plane = (size_t)s->pitch * s->real;
+    dfree(s->d_traj);
+    dfree(s->d_lam);
+    dfree(s->d_mu);
+    dfree(s->d_gfield);
+    dfree(s->d_gg);
+    dfree(s->d_probe_col);
+    dfree(s->d_fsteps);
+    dfree(s->d_bsteps);
+    CK(s, cudaMalloc(&s->d_traj, plane * s->cfg.n_state * seg_steps));
+    CK(s, cudaMalloc(&s->d_lam, plane * s->cfg.n_state));
+    CK(s, cudaMalloc(&s->d_mu, plane * 2));
+    CK(s, cudaMalloc(&s->d_gfield, plane * std::max(s->cfg.n_field, 1)));
+    CK(s, cudaMalloc(&s->d_gg, plane * 2));
+    CK(s, cudaMalloc((void **)&s->d_probe_col, s->pitch * sizeof(int)));
+    CK(s, cudaMalloc((void **)&s->d_fsteps, seg_steps * sizeof(mkg_step)));
+    CK(s, cudaMalloc((void **)&s->d_bsteps, seg_steps * sizeof(mkg_step)));
+    s->adj_seg = seg_steps;
+    return MKG_OK;
+}
+
+extern "C" int mkg_adj_forward(mkg_sim *s, double tmin, double tmax,
+                               double dt, double log_interval,
+                               int64_t *rows_out)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (!s->adj_lib) return set_err(s, MKG_ERR_ORDER, "mkg_adj_attach first");
+    int r = mkg_run_begin(s, tmin, tmax, dt, log_interval);
+    if (r) return r;
+    s->adj_sched.clear();
+    s->adj_seg_start.clear();
+    s->adj_seg_len.clear();
+    s->adj_seg_vsel.clear();
+    s->adj_log.clear();
+    s->adj_rows = 0;
+    const size_t plane = (size_t)s->pitch * s->real;
+    const size_t ckpt_bytes = plane * (s->cfg.n_state + 1);
+    size_t nseg = 0;
+    int status = MKG_OK;
+    while (status == MKG_OK) {
+        /* Checkpoint: state planes and the current V plane */
+        if (nseg >= s->adj_ckpt.size()) {
+            void *p = nullptr;
+            CK(s, cudaMalloc(&p, ckpt_bytes));
+            s->adj_ckpt.push_back(p);
+        }
+        char *ck = (char *)s->adj_ckpt[nseg];
+        CK(s, cudaMemcpyAsync(ck, s->d_state, plane * s->cfg.n_state,
+                              cudaMemcpyDeviceToDevice, s->stream));
+        CK(s, cudaMemcpyAsync(ck + plane * s->cfg.n_state,
+                              (char *)s->d_vbuf + (size_t)s->v_sel * plane,
+                              plane, cudaMemcpyDeviceToDevice, s->stream));
+        s->adj_seg_vsel.push_back(s->v_sel);
+        double t = 0;
+        int64_t rows = 0;
+        status = mkg_run_chunk(s, s->adj_seg, &t, &rows);
+        if (status < 0) return status;
+        if (status == MKG_HALT_NAN)
+            return set_err(s, MKG_ERR_ARG,
+                           "NaN in the forward pass of the adjoint");
+        const long long done = s->last_cell_steps / s->ncell;
+        s->adj_seg_start.push_back((long long)s->adj_sched.size());
+        s->adj_seg_len.push_back(done);
+        for (long long i = 0; i < done; ++i) {
+            mkg_step st = s->h_steps[i];
+            if (st.log_row >= 0) st.log_row += (int)s->adj_rows;
+            s->adj_sched.push_back(st);
+        }
+        s->adj_log.insert(s->adj_log.end(), s->h_log,
+                          s->h_log + rows * s->log_ncol);
+        s->adj_rows += rows;
+        nseg++;
+    }
+    if (rows_out) *rows_out = s->adj_rows;
+    return MKG_OK;
+}
+
+extern "C" int mkg_adj_read_log(mkg_sim *s, double *values, int64_t rows)
+{
+    if (!s || !values) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (rows != s->adj_rows)
+        return set_err(s, MKG_ERR_ARG, "expected %lld rows",
+                       (long long)s->adj_rows);
+    memcpy(values, s->adj_log.data(), rows * s->log_ncol * sizeof(double));
+    return MKG_OK;
+}
+
+namespace {
+
+template <typename Real>
+__global__ void k_sum_planes(const Real *__restrict__ in, long long n,
+                             long long pitch, double *out)
+{
+    /* out[p] = sum over the first n entries of plane p (one block per
+     * plane, fixed order: deterministic) */
+    __shared__ double part[256];
+    const Real *x = in + (long long)blockIdx.x * pitch;
+    double acc = 0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) acc += (double)x[i];
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = part[0];
+}
+
+int launch_coop(mkg_sim *s, cudaKernel_t k, void *arg, int occ,
+                long long need)
+{
+    cudaLaunchConfig_t lc;
+    memset(&lc, 0, sizeof(lc));
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    lc.blockDim = dim3(s->cfg.block_x * s->cfg.block_y, 1, 1);
+    lc.gridDim = dim3((unsigned)std::min<long long>(
+        need, (long long)occ * s->num_sms), 1, 1);
+    lc.stream = s->stream;
+    void *args[] = {arg};
+    CK(s, cudaLaunchKernelExC(&lc, (const void *)k, args));
+    s->n_launches++;
+    return MKG_OK;
+}
+
+template <typename Real>
+int adj_backward(mkg_sim *s, const double *lgrad, int64_t rows,
+                 double *grad_fields, double *grad_g)
+{
+    const size_t plane = (size_t)s->pitch * s->real;
+    const int ncol = s->log_ncol;
+    /* Loss gradient (as Real) and the probe column of each cell */
+    dfree(s->d_lgrad);
+    const long long nl = std::max<long long>(rows * ncol, 1);
+    CK(s, cudaMalloc(&s->d_lgrad, nl * s->real));
+    if (rows * ncol > 0) {
+        int r = upload_real<Real>(s, lgrad, rows * ncol, s->d_lgrad);
+        if (r) return r;
+    }
+    std::vector<int> pc(s->pitch, -1);
+    for (int j = 0; j < ncol; ++j) {
+        if (s->h_log_item[j] != s->cfg.i_vm)
+            return set_err(s, MKG_ERR_ARG,
+                           "the adjoint loss needs V columns only");
+        if (pc[s->h_log_cell[j]] >= 0)
+            return set_err(s, MKG_ERR_ARG, "cell logged twice");
+        pc[s->h_log_cell[j]] = j;
+    }
+    CK(s, cudaMemcpyAsync(s->d_probe_col, pc.data(), pc.size() * sizeof(int),
+                          cudaMemcpyHostToDevice, s->stream));
+    CK(s, cudaMemsetAsync(s->d_lam, 0, plane * s->cfg.n_state, s->stream));
+    CK(s, cudaMemsetAsync(s->d_mu, 0, plane * 2, s->stream));
+    CK(s, cudaMemsetAsync(s->d_gfield, 0,
+                          plane * std::max(s->cfg.n_field, 1), s->stream));
+    CK(s, cudaMemsetAsync(s->d_gg, 0, plane * 2, s->stream));
+    int mu_sel = 0;
+    std::vector<mkg_step> fsteps(s->adj_seg), bsteps(s->adj_seg);
+    mkg_status init;
+    init.barrier = 0;
+    init.error = MKG_DEV_OK;
+    init.halt_step = MKG_NO_HALT;
+    init.timeout_block = -1;
+    for (long long g = (long long)s->adj_seg_len.size() - 1; g >= 0; --g) {
+        const long long n = s->adj_seg_len[g];
+        if (n == 0) continue;
+        const long long st0 = s->adj_seg_start[g];
+        for (long long i = 0; i < n; ++i) {
+            bsteps[i] = s->adj_sched[st0 + i];
+            fsteps[i] = bsteps[i];
+            fsteps[i].log_row = -1;
+        }
+        /* Restore the segment's checkpoint */
+        const char *ck = (const char *)s->adj_ckpt[g];
+        const int vsel = s->adj_seg_vsel[g];
+        CK(s, cudaMemcpyAsync(s->d_state, ck, plane * s->cfg.n_state,
+                              cudaMemcpyDeviceToDevice, s->stream));
+        CK(s, cudaMemcpyAsync((char *)s->d_vbuf + (size_t)vsel * plane,
+                              ck + plane * s->cfg.n_state, plane,
+                              cudaMemcpyDeviceToDevice, s->stream));
+        CK(s, cudaMemcpyAsync(s->d_fsteps, fsteps.data(),
+                              n * sizeof(mkg_step), cudaMemcpyHostToDevice,
+                              s->stream));
+        CK(s, cudaMemcpyAsync(s->d_bsteps, bsteps.data(),
+                              n * sizeof(mkg_step), cudaMemcpyHostToDevice,
+                              s->stream));
+        /* Forward over the segment, recording the trajectory */
+        mkg_launch a;
+        fill_launch(s, &a);
+        a.n_log_items = 0;
+        a.log_ncol = 0;
+        a.nan_check = 0;
+        a.steps = s->d_fsteps;
+        a.nsteps = (int)n;
+        a.v_sel = vsel;
+        a.traj = s->d_traj;
+        *s->h_status = init;
+        CK(s, cudaMemcpyAsync(s->d_status, s->h_status, sizeof(mkg_status),
+                              cudaMemcpyHostToDevice, s->stream));
+        int r = launch_coop(s, s->adj_fwd, &a, s->adj_occ_fwd,
+                            blocks_needed(s, &a));
+        if (r) return r;
+        /* The segment in reverse */
+        mkg_adj_launch b;
+        memset(&b, 0, sizeof(b));
+        b.f = a;
+        b.f.steps = s->d_bsteps;
+        b.f.traj = nullptr;
+        b.traj = s->d_traj;
+        b.lam = s->d_lam;
+        b.mu = s->d_mu;
+        b.gfield = s->d_gfield;
+        b.gg = s->d_gg;
+        b.probe_col = s->d_probe_col;
+        b.lgrad = s->d_lgrad;
+        b.nprobe = ncol;
+        b.mu_sel = mu_sel;
+        CK(s, cudaMemcpyAsync(s->d_status, s->h_status, sizeof(mkg_status),
+                              cudaMemcpyHostToDevice, s->stream));
+        r = launch_coop(s, s->adj_bwd, &b, s->adj_occ_bwd,
+                        blocks_needed(s, &a));
+        if (r) return r;
+        mu_sel ^= (int)(n & 1);
+        CK(s, cudaMemcpyAsync(s->h_status, s->d_status, sizeof(mkg_status),
+                              cudaMemcpyDeviceToHost, s->stream));
+        CK(s, cudaStreamSynchronize(s->stream));
+        if (s->h_status->error != MKG_DEV_OK)
+            return set_err(s, MKG_ERR_TIMEOUT,
+                           "device barrier wait timed out in the adjoint");
+    }
+    /* Field gradients (AoS doubles) and the conductance gradients */
+    if (grad_fields && s->cfg.n_field > 0) {
+        int r = download_soa<Real>(s, grad_fields, s->cfg.n_field,
+                                   s->d_gfield, plain_slots(), nullptr);
+        if (r) return r;
+    }
+    if (grad_g) {
+        double *d_out = nullptr;
+        CK(s, cudaMalloc((void **)&d_out, 2 * sizeof(double)));
+        s->n_launches++;
+        k_sum_planes<Real><<<2, 256, 0, s->stream>>>(
+            (const Real *)s->d_gg, s->ncell, s->pitch, d_out);
+        cudaError_t e = cudaMemcpyAsync(grad_g, d_out, 2 * sizeof(double),
+                                        cudaMemcpyDeviceToHost, s->stream);
+        cudaStreamSynchronize(s->stream);
+        cudaFree(d_out);
+        if (e != cudaSuccess)
+            return set_err(s, MKG_ERR_CUDA, "gradient copy failed");
+    }
+    return MKG_OK;
+}
+
+}  // namespace
+
+extern "C" int mkg_adj_backward(mkg_sim *s, const double *lgrad,
+                                int64_t rows, double *grad_fields,
+                                double *grad_g)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (!s->adj_lib) return set_err(s, MKG_ERR_ORDER, "mkg_adj_attach first");
+    if (rows != s->adj_rows)
+        return set_err(s, MKG_ERR_ARG, "expected %lld rows",
+                       (long long)s->adj_rows);
+    if (rows * s->log_ncol > 0 && !lgrad)
+        return set_err(s, MKG_ERR_ARG, "null loss gradient");
+    if (s->real == 4)
+        return adj_backward<float>(s, lgrad, rows, grad_fields, grad_g);
+    return adj_backward<double>(s, lgrad, rows, grad_fields, grad_g);
 }

@@ -27,9 +27,9 @@ typedef struct mkg_step {
 
 /* Device-side status word, one per simulation. */
 typedef struct mkg_status {
-    unsigned int barrier;   /* grid barrier arrival counter (reset per launch) */
+    unsigned int barrier;   /* grid barrier arrival counter (reset per chunk) */
     int error;              /* MKG_DEV_* */
-    int halt_step;          /* first step of the launch that saw the NaN halt */
+    int halt_step;          /* first step of the chunk that saw the NaN halt */
     int timeout_block;      /* block that gave up waiting, for diagnostics */
 } mkg_status;
 
@@ -61,10 +61,8 @@ typedef struct mkg_launch {
     int log_ncol;
     int n_log_items;
     int nan_check;           /* apply the NaN halt at log rows */
-    int ntiles_x, ntiles_y;  /* tiles covering the grid (2D) or cells (1D) */
-    int stage_tiles;         /* 2D: tiles whose V halo tiles are staged in
-                                shared memory per __syncthreads (the
-                                dynamic shared memory holds this many) */
+    int ntiles_x, ntiles_y;  /* warp tiles (32 cells) per row, and rows */
+    int stage_tiles;         /* reserved */
     int step0;               /* index of this launch's first step within
                                 the chunk (for the NaN halt) */
     int epoch_base;          /* grid barriers completed by earlier launches
@@ -74,7 +72,23 @@ typedef struct mkg_launch {
     void *hi;                /* accumulation planes [n_hi][pitch], 8 bytes
                                 per entry: FP64 states, or FP32 Kahan
                                 compensation terms */
+    void *traj;              /* adjoint forward pass only: the states at t
+                                of every step, Real[nsteps][n_state][pitch] */
 } mkg_launch;
+
+/* Arguments of the adjoint kernel: one checkpoint segment in reverse. */
+typedef struct mkg_adj_launch {
+    mkg_launch f;            /* geometry, fields, pacing, schedule, status */
+    const void *traj;        /* Real[nsteps][n_state][pitch] */
+    void *lam;               /* Real[n_state][pitch]: own part of lambda */
+    void *mu;                /* Real[2][pitch]: dL/d idiff, double buffered */
+    void *gfield;            /* Real[n_field][pitch]: field gradients */
+    void *gg;                /* Real[2][pitch]: dL/dgx and dL/dgy per cell */
+    const int *probe_col;    /* int[pitch]: loss column of a cell or -1 */
+    const void *lgrad;       /* Real[rows][nprobe]: dL/dV at logged points */
+    int nprobe;
+    int mu_sel;              /* plane of mu holding mu_{k+1} at entry */
+} mkg_adj_launch;
 
 /* Accumulation modes for selected states of a single precision kernel */
 #define MKG_HI_NONE   0

@@ -302,7 +302,7 @@ class TissueKernel(object):
     def __init__(self, model, precision, native_math, bound_variables,
                  inter_log, diffusion, two_d, fields, rl_states, block,
                  fast_divide=True, min_blocks=1, math='default',
-                 accumulate=None, accumulate_states=()):
+                 accumulate=None, accumulate_states=(), traj=False):
         self.model = model
         self.single = (precision == myokit.SINGLE_PRECISION)
         self.native_math = bool(native_math)
@@ -340,6 +340,7 @@ class TissueKernel(object):
         self.hi_index = {i: j for j, i in enumerate(self.hi_states)}
         self.v_double = (self.accumulate == 'double' and
                          self.i_vm in self.hi_index)
+        self.traj = bool(traj)
         self.census = OpCensus()
         self._source = self._generate()
 
@@ -424,6 +425,13 @@ class TissueKernel(object):
         tab = '        '
 
         # Per-cell constants (fields and what depends on them), in order
+        # Recorded for the adjoint exporter: per-cell constant equations and
+        # the right-hand side equations, in evaluation order, with constants
+        # folded (lists of (lhs, folded rhs)).
+        self.writer = w
+        self.literal_subst = literal_subst
+        self.cell_const_eqs = []
+        self.rhs_eqs = []
         body.append(tab + '// Per-cell constants (scalar fields)')
         for k, var in enumerate(self.fields):
             body.append(
@@ -433,6 +441,7 @@ class TissueKernel(object):
             var = eq.lhs.var()
             if var in percell_const and var not in field_set:
                 rhs = fold(eq.rhs)
+                self.cell_const_eqs.append((eq.lhs, rhs))
                 self.census.add(rhs)
                 body.append(
                     f'{tab}const Real {self._name(var)} = {w.ex(rhs)};')
@@ -522,6 +531,7 @@ class TissueKernel(object):
                         var in self.rl_states:
                     continue
                 rhs = fold(eq.rhs)
+                self.rhs_eqs.append((eq.lhs, rhs))
                 self.census.add(rhs)
                 name = self._name(eq.lhs)
                 body.append(f'{tab}const Real {name} = {w.ex(rhs)};')
@@ -530,6 +540,14 @@ class TissueKernel(object):
         if len(emitted) != len(updates):   # pragma: no cover
             raise ValueError('Could not order the state updates.')
         self._inter_names = [self._name(v) for v in self.inter_log]
+
+        if self.traj:
+            # The adjoint's forward pass records the states at t of every
+            # step of the launch: traj[k][state][pitch]
+            for i, st in enumerate(self.states):
+                loads.append(
+                    f'{tab}((Real *)a.traj)[((long long)k * {self.n_state}'
+                    f' + {i}) * pitch + cid] = {self._name(st)};')
 
         # Logging: states and idiff right after the loads, intermediaries
         # at the end (item ids as in include/mkg_tissue.h).

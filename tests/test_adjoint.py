@@ -1,0 +1,189 @@
+"""
+The discrete adjoint: local symbolic partials (CPU), kernel generation for
+sm_103a (CPU, NVRTC), and on the GPU the gradients of a loss on probe V
+against central finite differences (relative step 1e-4, double precision),
+checkpoint-length independence and the torch.autograd.Function.
+"""
+import numpy as np
+import pytest
+
+from conftest import load, myokit
+import myokit_gb300 as mg
+from myokit_gb300 import _lib, adjoint, exporter
+
+DP = myokit.DOUBLE_PRECISION
+SP = myokit.SINGLE_PRECISION
+
+
+def _numeric_partial(e, ref, values):
+    h = 1e-6 * max(abs(values[ref]), 1e-9)
+
+    def ev(delta):
+        sub = {k: myokit.Number(v + (delta if k == ref else 0))
+               for k, v in values.items()}
+        return e.eval(subst=sub)
+    return (ev(h) - ev(-h)) / (2 * h)
+
+
+@pytest.mark.parametrize('name', ['beeler-1977-model.mmt', 'lr-1991.mmt'])
+def test_local_partials_match_numerical(name):
+    m = load(name)
+    rng = np.random.default_rng(0)
+    checked = 0
+    for v in m.variables(deep=True):
+        if v.is_state() or v.is_constant() or v.is_bound():
+            continue
+        e = v.rhs()
+        refs = [r for r in adjoint._references(e)]
+        if not refs:
+            continue
+        values = {}
+        for r in refs:
+            rv = r.var()
+            if rv.is_state():
+                values[r] = rv.initial_value(True) * (1 + 0.1 * rng.normal())
+            else:
+                values[r] = rv.eval() if rv.is_constant() else rng.uniform(
+                    0.5, 2)
+        for r in refs:
+            dp = adjoint.local_partial(e, r)
+            sub = {k: myokit.Number(x) for k, x in values.items()}
+            a = 0.0 if dp is None else dp.eval(subst=sub)
+            b = _numeric_partial(e, r, values)
+            assert abs(a - b) <= 1e-5 * max(1e-8, abs(b)), (v.qname(), r)
+            checked += 1
+    assert checked > 20
+
+
+def _sim(model, precision, shape=(6, 5), rl=False, fields=None):
+    p = myokit.pacing.blocktrain(period=1000, duration=2, offset=1)
+    s = mg.SimulationCUDA(model, p, ncells=shape, precision=precision, rl=rl)
+    s.set_paced_cells(2, shape[1] if isinstance(shape, tuple) else 1)
+    s.set_conductance(9, 6)
+    for name, values in (fields or {}).items():
+        s.set_field(name, values)
+    return s
+
+
+@pytest.mark.parametrize('name,field', [
+    ('beeler-1977-model.mmt', 'isi.gsBar'),
+    ('decker-2009.mmt', 'ikr.Gbar'),
+])
+@pytest.mark.parametrize('precision', [SP, DP])
+def test_adjoint_kernels_compile(name, field, precision):
+    m = load(name)
+    base = m.get(field).eval()
+    s = _sim(m, precision, rl=True, fields={field: np.full((5, 6), base)})
+    k = s._kernel([])
+    fwd = exporter.TissueKernel(
+        s._model, s._precision, False, s._bound_variables, [], k.diffusion,
+        k.two_d, list(s._fields.keys()), s._rl_states, k.block, traj=True)
+    ak = adjoint.AdjointKernel(fwd)
+    cubin, _ = _lib.compile_source(ak.source(), ak.options())
+    assert cubin[:4] == b'\x7fELF'
+    assert 'mkg_tissue_adjoint' in ak.source()
+
+
+def _fields(m, shape, seed):
+    rng = np.random.default_rng(seed)
+    return {
+        'isi.gsBar': m.get('isi.gsBar').eval() * rng.lognormal(0, 0.2, shape),
+        'ina.gNaBar': m.get('ina.gNaBar').eval() * rng.lognormal(0, 0.2,
+                                                                  shape),
+    }
+
+
+PROBES = [(0, 0), (3, 2), (5, 4), (1, 4)]
+
+
+def _loss(s, adj, target, dur=12):
+    v = adj.forward(dur, 0.5)
+    return float(np.sum((v - target) ** 2))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('rl', [False, True])
+def test_adjoint_matches_finite_differences(br77, rl):
+    shape = (5, 6)
+    f0 = _fields(br77, shape, 1)
+    ft = _fields(br77, shape, 2)
+    s = _sim(br77, DP, rl=rl, fields=ft)
+    adj = adjoint.TissueAdjoint(s, PROBES, segment_steps=150)
+    target = adj.forward(12, 0.5)
+    for k, v in f0.items():
+        s.set_field(k, v)
+    s.set_conductance(8, 5)
+    L, grads = adj.loss_and_gradient(12, target, 0.5)
+    assert L > 0
+    rng = np.random.default_rng(3)
+    checks = []
+    for name in f0:
+        for _ in range(3):
+            iy, ix = rng.integers(0, shape[0]), rng.integers(0, shape[1])
+            checks.append((name, (iy, ix)))
+    checks += [('gx', None), ('gy', None)]
+    for name, idx in checks:
+        if name in ('gx', 'gy'):
+            g0 = 8.0 if name == 'gx' else 5.0
+            h = 1e-4 * g0
+            vals = []
+            for sgn in (1, -1):
+                gx = g0 + sgn * h if name == 'gx' else 8.0
+                gy = g0 + sgn * h if name == 'gy' else 5.0
+                s.set_conductance(gx, gy)
+                vals.append(_loss(s, adj, target))
+            s.set_conductance(8, 5)
+            fd = (vals[0] - vals[1]) / (2 * h)
+            ad = grads[name]
+        else:
+            base = f0[name].copy()
+            h = 1e-4 * base[idx]
+            vals = []
+            for sgn in (1, -1):
+                f = base.copy()
+                f[idx] += sgn * h
+                s.set_field(name, f)
+                vals.append(_loss(s, adj, target))
+            s.set_field(name, base)
+            fd = (vals[0] - vals[1]) / (2 * h)
+            ad = grads[name][idx]
+        scale = max(abs(fd), 1e-6 * abs(L))
+        assert abs(ad - fd) <= 1e-4 * scale, (name, idx, ad, fd)
+
+
+@pytest.mark.gpu
+def test_adjoint_checkpoint_length_independent(br77):
+    shape = (5, 6)
+    s = _sim(br77, DP, fields=_fields(br77, shape, 1))
+    target = np.zeros((24, len(PROBES))) - 80
+    out = []
+    for k in (7, 64, 1000):
+        adj = adjoint.TissueAdjoint(s, PROBES, segment_steps=k)
+        L, g = adj.loss_and_gradient(12, target, 0.5)
+        out.append((L, g))
+    for L, g in out[1:]:
+        assert L == out[0][0]
+        for k in g:
+            assert np.array_equal(np.asarray(g[k]), np.asarray(out[0][1][k]))
+
+
+@pytest.mark.gpu
+def test_torch_function_gradients(br77):
+    import torch
+    shape = (5, 6)
+    f0 = _fields(br77, shape, 1)
+    s = _sim(br77, DP, fields=f0)
+    adj = adjoint.TissueAdjoint(s, PROBES, segment_steps=100)
+    target = torch.full((24, len(PROBES)), -80.0, dtype=torch.float64)
+    g = torch.tensor(7.0, dtype=torch.float64, requires_grad=True)
+    fields = [torch.tensor(f0[n], requires_grad=True)
+              for n in adj.field_names()]
+    loss = adjoint.tissue_loss(adj, 12, target, g, fields, 0.5)
+    loss.backward()
+    s.set_conductance(7, 7)
+    L, ref = adj.loss_and_gradient(12, target.numpy(), 0.5)
+    assert abs(loss.item() - L) <= 1e-12 * abs(L)
+    assert abs(float(g.grad) - (ref['gx'] + ref['gy'])) <= 1e-12 * abs(
+        ref['gx'] + ref['gy'])
+    for t, n in zip(fields, adj.field_names()):
+        np.testing.assert_allclose(t.grad.numpy(), ref[n], rtol=1e-12)
