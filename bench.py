@@ -63,6 +63,9 @@ def parse():
     p.add_argument('--accuracy-ms', type=float, default=400.0,
                    help='simulated time of the precision comparison runs'
                         ' (0 = skip)')
+    p.add_argument('--adjoint-ms', type=float, default=100.0,
+                   help='simulated time of the adjoint measurement'
+                        ' (0 = skip)')
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-seconds', type=float, default=12.0,
                    help='target CPU work for the cpu_baseline sample')
@@ -283,6 +286,104 @@ def accuracy_runs(args, device):
     return out
 
 
+def adjoint_runs(args, device):
+    """
+    The discrete adjoint on a 256 x 256 sheet of the bench configuration
+    (single precision): loss = sum of squared V errors at 64 probes every
+    1 ms against a target made with seed-perturbed GKr/GNa fields; gradient
+    with respect to both fields and gx, gy; checkpoints every 200 steps.
+    Reports adjoint time / forward time, and a central finite-difference
+    check (relative step 1e-4, double precision, 64 x 64 sheet, 20 random
+    entries).
+    """
+    import torch
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+    from myokit_gb300 import adjoint as ad
+    out = {}
+    n = 256
+    dur = args.adjoint_ms
+    rng = np.random.default_rng(5)
+    cells = rng.choice(n * n, 64, replace=False)
+    probes = [(int(c % n), int(c // n)) for c in cells]
+    keys = ['%d.%d.membrane.V' % p for p in probes]
+    s, _ = make_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION, n,
+                      seed=1, device=device)
+    adj = ad.TissueAdjoint(s, probes, segment_steps=200)
+    target = adj.forward(dur, 1.0)
+    s, _ = make_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION, n,
+                      seed=0, device=device)
+    adj = ad.TissueAdjoint(s, probes, segment_steps=200)
+    adj.loss_and_gradient(min(dur, 5.0), target[:int(min(dur, 5.0))], 1.0)
+    s.run(min(dur, 5.0), log=['engine.time'] + keys, log_interval=1)
+    s.reset()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.run(dur, log=['engine.time'] + keys, log_interval=1)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    s.reset()
+    t0 = time.perf_counter()
+    v = adj.forward(dur, 1.0)
+    t1 = time.perf_counter()
+    grads = adj.backward(2 * (v - target))
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    out['sheet256_fp32'] = {
+        'window_ms': dur, 'probes': len(probes), 'segment_steps': 200,
+        'forward_s': t_fwd, 'adjoint_forward_s': t1 - t0,
+        'adjoint_backward_s': t2 - t1,
+        'adjoint_over_forward': (t2 - t0) / t_fwd,
+        'loss': float(np.sum((v - target) ** 2)),
+        'grad_norm_gkr': float(np.linalg.norm(grads['ikr.Gbar'])),
+        'grad_gx': grads['gx'], 'grad_gy': grads['gy'],
+    }
+
+    # Finite-difference check in double precision on a 64 x 64 sheet
+    n = 64
+    fd_ms = min(dur, 50.0)
+    cells = rng.choice(n * n, 16, replace=False)
+    probes = [(int(c % n), int(c // n)) for c in cells]
+    s, _ = make_sheet(mg.SimulationCUDA, myokit.DOUBLE_PRECISION, n,
+                      seed=1, device=device)
+    adj = ad.TissueAdjoint(s, probes, segment_steps=200)
+    target = adj.forward(fd_ms, 1.0)
+    s, _ = make_sheet(mg.SimulationCUDA, myokit.DOUBLE_PRECISION, n,
+                      seed=0, device=device)
+    adj = ad.TissueAdjoint(s, probes, segment_steps=200)
+    L, grads = adj.loss_and_gradient(fd_ms, target, 1.0)
+    base = {k: np.array(s._fields[s._model.get(k)]).reshape(n, n)
+            for k in ('ikr.Gbar', 'ina.Gbar')}
+
+    def loss():
+        v = adj.forward(fd_ms, 1.0)
+        return float(np.sum((v - target) ** 2))
+    worst = 0.0
+    entries = []
+    for i in range(20):
+        name = ('ikr.Gbar', 'ina.Gbar')[i % 2]
+        iy, ix = int(rng.integers(0, n)), int(rng.integers(0, n))
+        f = base[name].copy()
+        h = 1e-4 * f[iy, ix]
+        vals = []
+        for sg in (1, -1):
+            g = f.copy()
+            g[iy, ix] += sg * h
+            s.set_field(name, g)
+            vals.append(loss())
+        s.set_field(name, f)
+        fd = (vals[0] - vals[1]) / (2 * h)
+        a = grads[name][iy, ix]
+        rel = abs(a - fd) / max(abs(fd), 1e-12 * abs(L))
+        worst = max(worst, rel)
+        entries.append({'field': name, 'cell': [ix, iy], 'adjoint': a,
+                        'fd': fd, 'rel_err': rel})
+    out['fd_check_sheet64_fp64'] = {
+        'window_ms': fd_ms, 'entries': len(entries),
+        'max_rel_err': worst, 'loss': L, 'sample': entries[:4]}
+    return out
+
+
 def run_reference(args):
     """--impl reference: the reference kernel on the host cores."""
     rank = int(os.environ.get('RANK', '0'))
@@ -469,6 +570,10 @@ def run_ours(args):
     if args.accuracy_ms > 0 and rank == 0:
         accuracy.update(accuracy_runs(args, local))
 
+    adj = None
+    if args.adjoint_ms > 0 and rank == 0:
+        adj = adjoint_runs(args, local)
+
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline(args, myokit.SINGLE_PRECISION, args.cpu_seconds)
@@ -502,6 +607,7 @@ def run_ours(args):
         'fp64': fp64,
         'variants': variants,
         'accuracy': accuracy,
+        'adjoint': adj,
         'clocks': clocks,
         'cpu_baseline': cpu,
     }

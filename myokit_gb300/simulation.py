@@ -267,6 +267,9 @@ class SimulationCUDA(object):
         self._graphs = 1
         self._tune_sig = None
         self._tune_hit = None
+        self._model_version = 0
+        self._log_templates = {}
+        self._kernels = {}
         self._device = int(device)
         self._backend = None
         self._last_stats = None
@@ -566,6 +569,7 @@ class SimulationCUDA(object):
             raise ValueError(
                 'The given variable <' + var.qname() + '> is not a literal.')
         self._model.set_value(var.qname(), value)
+        self._model_version += 1
 
     def set_field(self, var, values):
         """
@@ -739,9 +743,11 @@ class SimulationCUDA(object):
     def _tuned_choice(self):
         """A cached autotuner result for this configuration, or None."""
         from . import autotune
-        sig = autotune.signature(self)
-        if self._tune_sig != sig:
-            self._tune_sig = sig
+        key = (self._model_version, self._precision, self._accumulate,
+               self._fp32_math, self._native_math, self._diffusion_mode(),
+               tuple(v.qname() for v in self._fields))
+        if self._tune_sig != key:
+            self._tune_sig = key
             self._tune_hit = autotune.lookup(self)
         return self._tune_hit
 
@@ -815,18 +821,31 @@ class SimulationCUDA(object):
         return out
 
     def _kernel(self, inter_log):
-        """The generated kernel for the current configuration."""
+        """The generated kernel for the current configuration (cached)."""
         mode = self._diffusion_mode()
         two_d = len(self._dims) == 2 and mode in (
             _exp.DIFF_GRID, _exp.DIFF_HETERO)
         block = self._block_shape(two_d)
-        return _exp.TissueKernel(
-            self._model, self._precision, self._native_math,
-            self._bound_variables, inter_log, mode, two_d,
-            list(self._fields.keys()), self._rl_states, block,
-            min_blocks=self._default_min_blocks(block),
-            math=self._fp32_math, accumulate=self._accumulate,
-            accumulate_states=self.accumulated_states())
+        minb = self._default_min_blocks(block)
+        acc = self.accumulated_states()
+        key = (
+            self._model_version, self._precision, self._native_math, mode,
+            two_d, block, minb, self._fp32_math, self._accumulate,
+            tuple(v.qname() for v in acc),
+            tuple(v.qname() for v in self._fields.keys()),
+            tuple(v.qname() for v in inter_log))
+        k = self._kernels.get(key)
+        if k is None:
+            k = _exp.TissueKernel(
+                self._model, self._precision, self._native_math,
+                self._bound_variables, inter_log, mode, two_d,
+                list(self._fields.keys()), self._rl_states, block,
+                min_blocks=minb, math=self._fp32_math,
+                accumulate=self._accumulate, accumulate_states=acc)
+            if len(self._kernels) > 16:
+                self._kernels.clear()
+            self._kernels[key] = k
+        return k
 
     def _get_backend(self, kernel):
         """A host-library handle for this kernel, reused between runs."""
@@ -911,6 +930,46 @@ class SimulationCUDA(object):
             sources.append((item, cell))
         return sources
 
+    def _prepare_log(self, log, global_vars):
+        """
+        ``myokit.prepare_log`` with the simulation's arguments
+        (openclsim.py:1033-1042). For a flag or a list of names, the empty
+        log it builds is remembered as a template (per model version), so a
+        repeated run does not re-validate every key against every cell.
+        """
+        key = None
+        if isinstance(log, int) and not isinstance(log, bool):
+            key = ('flag', log)
+        elif isinstance(log, (list, tuple)) and all(
+                isinstance(x, str) for x in log):
+            key = ('names', tuple(log))
+        elif log is None:
+            key = ('none',)
+        if key is not None:
+            key = key + (self._model_version, tuple(global_vars))
+            tpl = self._log_templates.get(key)
+            if tpl is not None:
+                out = myokit.DataLog(tpl)
+                tc = 'd' if self._precision == myokit.DOUBLE_PRECISION \
+                    else 'f'
+                for k in tpl.keys():
+                    OrderedDict.__setitem__(out, k, array.array(tc))
+                return out
+        out = myokit.prepare_log(
+            log,
+            self._model,
+            dims=self._dims,
+            global_vars=global_vars,
+            if_empty=myokit.LOG_STATE + myokit.LOG_BOUND,
+            allowed_classes=myokit.LOG_STATE + myokit.LOG_INTER
+            + myokit.LOG_BOUND,
+            precision=self._precision)
+        if key is not None:
+            if len(self._log_templates) > 32:
+                self._log_templates.clear()
+            self._log_templates[key] = myokit.DataLog(out)
+        return out
+
     def _run(self, duration, log, log_interval, report_nan, progress, msg):
         # Times (openclsim.py:1018-1024)
         if duration < 0:
@@ -923,15 +982,7 @@ class SimulationCUDA(object):
             v = self._model.binding(label)
             if v is not None:
                 g.append(v.qname())
-        log = myokit.prepare_log(
-            log,
-            self._model,
-            dims=self._dims,
-            global_vars=g,
-            if_empty=myokit.LOG_STATE + myokit.LOG_BOUND,
-            allowed_classes=myokit.LOG_STATE + myokit.LOG_INTER
-            + myokit.LOG_BOUND,
-            precision=self._precision)
+        log = self._prepare_log(log, g)
 
         # Logged intermediary variables (openclsim.py:1044-1053)
         inter_log = []
