@@ -66,6 +66,12 @@ def parse():
     p.add_argument('--adjoint-ms', type=float, default=100.0,
                    help='simulated time of the adjoint measurement'
                         ' (0 = skip)')
+    p.add_argument('--configs', default='c1,c3,c5',
+                   help='other BASELINE configurations to time (comma list'
+                        ' of c1, c3, c5; empty = none)')
+    p.add_argument('--c5-full', action='store_true',
+                   help='run the whole 1000 ms S1-S2 protocol of the'
+                        ' 2048x2048 sheet instead of a 20 ms window')
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-seconds', type=float, default=12.0,
                    help='target CPU work for the cpu_baseline sample')
@@ -384,6 +390,159 @@ def adjoint_runs(args, device):
     return out
 
 
+def config_c1(args, device):
+    """
+    Plain method, FP64: a 200-cell Beeler-Reuter 1977 cable, forward Euler,
+    dt 0.005 ms, g = 9, the first 5 cells paced at 1 Hz (2 ms pulses), V of
+    every cell logged every 1 ms, 1000 ms. Timed on the GPU in double
+    precision and single precision with Kahan accumulation; compared with
+    the reference's own Simulation1d (C, one host core) on a 100 ms window.
+    """
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+    path = os.path.join(os.path.dirname(myokit.__file__), 'tests', 'data',
+                        'beeler-1977-model.mmt')
+    m = myokit.load_model(path)
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    out = {'cells': 200, 'steps': 200000}
+
+    def setup(cls, **kw):
+        s = cls(m, p, ncells=200, **kw)
+        s.set_step_size(0.005)
+        s.set_conductance(9)
+        s.set_paced_cells(5)
+        return s
+    log = ['engine.time', 'membrane.V']
+    logs = {}
+    for name, kw in (('fp64', {'precision': myokit.DOUBLE_PRECISION}),
+                     ('fp32+kahan', {'precision': myokit.SINGLE_PRECISION,
+                                     'accumulate': 'kahan'})):
+        s = setup(mg.SimulationCUDA, device=device, **kw)
+        s.run(5, log=log, log_interval=1)
+        s.reset()
+        t0 = time.perf_counter()
+        d = s.run(1000, log=log, log_interval=1)
+        wall = time.perf_counter() - t0
+        st = s.last_run_stats()
+        logs[name] = d
+        out[name] = {'value': 200 * 200000 / (st['kernel_ms'] / 1000),
+                     'e2e': 200 * 200000 / wall, 'unit': UNIT,
+                     'wall_s': wall}
+    try:
+        sa = setup(myokit.Simulation1d)
+        t0 = time.perf_counter()
+        da = sa.run(100, log=log, log_interval=1)
+        wall = time.perf_counter() - t0
+    except Exception as e:  # the reference compiles C at run time
+        out['simulation1d_cpu'] = {'unavailable': str(e).splitlines()[0]}
+        return out
+    out['simulation1d_cpu'] = {'value': 200 * 20000 / wall, 'unit': UNIT,
+                               'cores': 1, 'window_ms': 100}
+    dv = {}
+    for name, d in logs.items():
+        dv[name] = max(float(np.max(np.abs(
+            np.asarray(da['membrane.V', c]) -
+            np.asarray(d['membrane.V', c])[:100]))) for c in range(200))
+    out['max_abs_dV_vs_simulation1d_mV'] = dv
+    return out
+
+
+def config_c3(args, device):
+    """
+    Batched: 512 independent cables of lengths uniform 50-2000 cells in one
+    1D simulation (zero conductance between cables), 6 conductances per
+    cable scaled lognormal(0, 0.3), dt 0.01 ms, the first 5 cells of each
+    cable paced at 1 Hz; single precision with Kahan-compensated V and
+    concentrations; launches of 100 steps replayed from CUDA graphs. The
+    Decker 2009 model stands in for ten Tusscher 2006. Timed over 20 ms.
+    """
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+    rng = np.random.default_rng(3)
+    lengths = rng.integers(50, 2001, 512)
+    n = int(lengths.sum())
+    starts = np.concatenate([[0], np.cumsum(lengths)[:-1]])
+    m = load_model()
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    names = ['ina.Gbar', 'inal.Gbar', 'ik1.Gbar', 'ikr.Gbar', 'ito.Gbar',
+             'ikur.Gbar']
+    out = {'cables': 512, 'cells': n}
+    for spl in (100, 0):
+        s = mg.SimulationCUDA(m, p, ncells=n, rl=True, accumulate='kahan',
+                              steps_per_launch=spl, device=device)
+        s.set_step_size(0.01)
+        g = np.full(n - 1, 10.0)
+        g[starts[1:] - 1] = 0
+        s.set_conductance_field(g)
+        for name in names:
+            base = m.get(name).eval()
+            s.set_field(name, np.repeat(
+                base * rng.lognormal(0, 0.3, 512), lengths))
+        s.set_paced_cell_list([int(a + k) for a in starts for k in range(5)])
+        s.run(2, log=['engine.time'], log_interval=1)
+        s.run(20, log=['engine.time'], log_interval=1)
+        st = s.last_run_stats()
+        out['steps_per_launch_%d' % spl] = {
+            'value': st['cell_steps'] / (st['kernel_ms'] / 1000),
+            'unit': UNIT, 'launches': st['launches'], 'window_ms': 20}
+    return out
+
+
+def config_c5(args, device):
+    """
+    Large: a 2048 x 2048 sheet, single precision with Kahan-compensated V
+    and concentrations, dt 0.005 ms; S1 on the left edge at t = 0, then S2
+    on the lower-left quadrant at t = 320 ms; the full V frame every 5 ms
+    recorded in a device buffer (run_frames). Timed over a 20 ms window,
+    or the whole 1000 ms with --c5-full.
+    """
+    import torch
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+    n = 2048
+    m = load_model()
+    s1 = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    s = mg.SimulationCUDA(m, s1, ncells=(n, n), rl=True, accumulate='kahan',
+                          device=device)
+    s.set_step_size(0.005)
+    s.set_paced_cells(nx=4, ny=n, x=0, y=0)
+    s.run_frames(1, 5)
+    s.reset()
+    out = {'grid': [n, n]}
+    torch.cuda.synchronize()
+    if args.c5_full:
+        t0 = time.perf_counter()
+        t1_, f1 = s.run_frames(320, 5)
+        ms = s.last_run_stats()['kernel_ms']
+        s.set_paced_cells(nx=n // 2, ny=n // 2, x=0, y=0)
+        p2 = myokit.Protocol()
+        p2.schedule(level=1, start=320, duration=2)
+        s.set_protocol(p2)
+        t2_, f2 = s.run_frames(680, 5)
+        ms += s.last_run_stats()['kernel_ms']
+        wall = time.perf_counter() - t0
+        frames = torch.cat([f1, f2])
+        steps = 200000
+        out.update({'window_ms': 1000, 'frames': int(frames.shape[0]),
+                    'frame_bytes': int(frames[0].numel() *
+                                       frames.element_size()),
+                    'final_v_range_mV': [float(frames[-1].min()),
+                                         float(frames[-1].max())],
+                    'activated_fraction_final': float(
+                        (frames[-1] > -40).float().mean())})
+    else:
+        t0 = time.perf_counter()
+        tt, frames = s.run_frames(20, 5)
+        wall = time.perf_counter() - t0
+        ms = s.last_run_stats()['kernel_ms']
+        steps = 4000
+        out.update({'window_ms': 20, 'frames': int(frames.shape[0])})
+    out['value'] = n * n * steps / (ms / 1000)
+    out['e2e'] = n * n * steps / wall
+    out['unit'] = UNIT
+    return out
+
+
 def run_reference(args):
     """--impl reference: the reference kernel on the host cores."""
     rank = int(os.environ.get('RANK', '0'))
@@ -574,6 +733,13 @@ def run_ours(args):
     if args.adjoint_ms > 0 and rank == 0:
         adj = adjoint_runs(args, local)
 
+    others = {}
+    wanted = [c for c in args.configs.split(',') if c]
+    if rank == 0:
+        for c in wanted:
+            others[c] = {'c1': config_c1, 'c3': config_c3,
+                         'c5': config_c5}[c](args, local)
+
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline(args, myokit.SINGLE_PRECISION, args.cpu_seconds)
@@ -608,6 +774,7 @@ def run_ours(args):
         'variants': variants,
         'accuracy': accuracy,
         'adjoint': adj,
+        'other_configs': others,
         'clocks': clocks,
         'cpu_baseline': cpu,
     }

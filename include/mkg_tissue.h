@@ -242,6 +242,17 @@ int mkg_adj_read_log(mkg_sim *sim, double *values, int64_t rows);
 int mkg_adj_backward(mkg_sim *sim, const double *lgrad, int64_t rows,
                      double *grad_fields, double *grad_g);
 
+/*
+ * Device frame buffer: when set (rows > 0), log rows are written by the
+ * kernel into dev_ptr (Real[rows][ncol], a device allocation owned by the
+ * caller, filled from row 0 on) and never copied to the host; mkg_read_log
+ * then returns times and pace only. For full-frame recordings (every cell's
+ * V every few ms) that would not fit a host round trip. No counterpart in
+ * the reference, which appends every logged value to a Python list
+ * (openclsim.c:1122-1131). dev_ptr NULL / rows 0 switches it off.
+ */
+int mkg_set_frame_buffer(mkg_sim *sim, void *dev_ptr, int64_t rows);
+
 /* The cudaStream_t (as void*) all work of this handle is queued on, so a
  * caller can time it with events recorded on the same stream. */
 int mkg_stream(const mkg_sim *sim, void **stream);

@@ -108,6 +108,8 @@ SIGNATURES = {
     'mkg_last_stats': (ctypes.c_int, [
         ctypes.c_void_p, _c_double_p, _c_int64_p, _c_int64_p]),
     'mkg_launch_count': (ctypes.c_int, [ctypes.c_void_p, _c_int64_p]),
+    'mkg_set_frame_buffer': (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
     'mkg_adj_attach': (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int32]),
     'mkg_adj_forward': (ctypes.c_int, [

@@ -206,6 +206,10 @@ struct mkg_sim {
     bool use_graphs = false;  /* replay multi-launch chunks as CUDA graphs */
     std::map<std::string, cudaGraphExec_t> graphs;
 
+    /* Device frame buffer for log rows (not owned) */
+    void *frame_buf = nullptr;
+    int64_t frame_rows = 0, frame_next = 0;
+
     /* Logged columns (host copy) */
     std::vector<int> h_log_item;
     std::vector<long long> h_log_cell;
@@ -287,7 +291,13 @@ int ensure_schedule(mkg_sim *s, int64_t steps, int64_t rows)
         s->h_tend.resize(steps);
         s->cap_steps = steps;
     }
-    if (rows > s->cap_rows) {
+    if ((int64_t)s->h_time.size() < rows) {
+        s->h_time.resize(rows);
+        s->h_pace.resize(rows);
+    }
+    /* Log values are staged on the device and copied back, unless a
+     * device frame buffer receives them. */
+    if (!s->frame_buf && rows > s->cap_rows) {
         dfree(s->d_log);
         dfree(s->d_log_dbl);
         if (s->h_log) cudaFreeHost(s->h_log);
@@ -297,8 +307,6 @@ int ensure_schedule(mkg_sim *s, int64_t steps, int64_t rows)
         CK(s, cudaMalloc(&s->d_log, n * s->real));
         CK(s, cudaMalloc((void **)&s->d_log_dbl, n * sizeof(double)));
         CK(s, cudaMallocHost((void **)&s->h_log, n * sizeof(double)));
-        s->h_time.resize(rows);
-        s->h_pace.resize(rows);
         s->cap_rows = rows;
     }
     return MKG_OK;
@@ -993,10 +1001,17 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
         return MKG_DONE;
     }
 
-    /* Log rows that fit a 256 MiB buffer, at least 16. */
+    /* Log rows that fit a 256 MiB buffer, at least 16; with a device frame
+     * buffer, the rows it has left. */
     const int64_t ncol = std::max(s->log_ncol, 1);
     int64_t row_cap = (int64_t)(256ll << 20) / (ncol * 8);
     row_cap = std::max<int64_t>(16, std::min<int64_t>(row_cap, max_steps));
+    if (s->frame_buf) {
+        row_cap = s->frame_rows - s->frame_next;
+        if (row_cap <= 0 && s->sched.next_logs())
+            return set_err(s, MKG_ERR_ARG, "the frame buffer is full");
+        row_cap = std::max<int64_t>(row_cap, 0);
+    }
     int r = ensure_schedule(s, max_steps, row_cap);
     if (r) return r;
 
@@ -1038,6 +1053,9 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
     const int bx = s->cfg.block_x, by = s->cfg.block_y;
     mkg_launch a;
     fill_launch(s, &a);
+    if (s->frame_buf)
+        a.log = (char *)s->frame_buf +
+                (size_t)s->frame_next * s->log_ncol * s->real;
     const int threads = bx * by;
     const long long nblocks = blocks_needed(s, &a);
     int bpsm = s->blocks_per_sm > 0 ? std::min(s->blocks_per_sm, s->occ_blocks)
@@ -1155,7 +1173,10 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
     int64_t rows_done = 0;
     for (int64_t i = 0; i < done; ++i)
         if (s->h_steps[i].log_row >= 0) rows_done = s->h_steps[i].log_row + 1;
-    if (rows_done > 0 && s->log_ncol > 0) {
+    if (s->frame_buf) {
+        /* Frames stay on the device */
+        s->frame_next += rows_done;
+    } else if (rows_done > 0 && s->log_ncol > 0) {
         const long long cnt = rows_done * (long long)s->log_ncol;
         s->n_launches++;
         if (s->real == 4)
@@ -1209,6 +1230,18 @@ int mkg_last_stats(const mkg_sim *s, double *kernel_ms, int64_t *launches,
     if (kernel_ms) *kernel_ms = s->last_ms;
     if (launches) *launches = s->last_launches;
     if (cell_steps) *cell_steps = s->last_cell_steps;
+    return MKG_OK;
+}
+
+int mkg_set_frame_buffer(mkg_sim *s, void *dev_ptr, int64_t rows)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (rows < 0 || (rows > 0 && !dev_ptr))
+        return set_err(s, MKG_ERR_ARG, "invalid frame buffer");
+    clear_graphs(s);
+    s->frame_buf = rows > 0 ? dev_ptr : nullptr;
+    s->frame_rows = rows;
+    s->frame_next = 0;
     return MKG_OK;
 }
 

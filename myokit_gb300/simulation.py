@@ -1180,6 +1180,85 @@ class SimulationCUDA(object):
                 _extend(log[key], data)
         return status == _lib.MKG_HALT_NAN
 
+    def run_frames(self, duration, interval=5.0, variable=None):
+        """
+        Runs for ``duration`` time units and records ``variable`` (a state;
+        by default the membrane potential) of every cell every ``interval``
+        time units into a CUDA tensor that never leaves the device. Returns
+        ``(times, frames)``: a numpy array of the frame times and a torch
+        tensor shaped ``(n_frames, ny, nx)`` (``(n_frames, nx)`` in 1d) in
+        the simulation precision. Time and state advance as in :meth:`run`;
+        the NaN check of logged runs does not apply.
+        """
+        import torch
+        if duration < 0:
+            raise ValueError('Simulation time can\'t be negative.')
+        interval = float(interval)
+        if interval <= 0:
+            raise ValueError('The frame interval must be positive.')
+        var = self._vm if variable is None else self._model.get(
+            variable.qname() if isinstance(variable, myokit.Variable)
+            else variable)
+        if var is None or not var.is_state():
+            raise ValueError('Frames record a state variable.')
+        cap = int(np.ceil(duration / interval)) + 1
+        dtype = torch.float32 if self._precision == myokit.SINGLE_PRECISION \
+            else torch.float64
+        frames = torch.empty((cap, self._ntotal), dtype=dtype,
+                             device='cuda:%d' % self._device)
+        kernel = self._kernel([])
+        self._last_kernel = kernel
+        be = self._get_backend(kernel)
+        lib, h = be.lib, be.h
+        tmin = self._time
+        times = []
+        if duration > 0:
+            self._upload(be)
+            items = np.full(self._ntotal, var.index(), dtype=np.int32)
+            cells = np.arange(self._ntotal, dtype=np.int64)
+            be.check(lib.mkg_set_log(h, _lib.i32ptr(items),
+                                     _lib.i64ptr(cells), len(cells), 0))
+            be.check(lib.mkg_set_tuning(h, self._launch_steps(),
+                                        self._blocks_per_sm, self._graphs))
+            torch.cuda.synchronize(self._device)
+            be.check(lib.mkg_set_frame_buffer(
+                h, _lib.ctypes.c_void_p(frames.data_ptr()), cap))
+            try:
+                be.check(lib.mkg_run_begin(h, tmin, tmin + duration,
+                                           self._step_size, interval))
+                t_out = _lib.ctypes.c_double()
+                rows = _lib.ctypes.c_int64()
+                status = _lib.MKG_OK
+                ms = 0.0
+                cs = 0
+                while status == _lib.MKG_OK:
+                    status = be.check(lib.mkg_run_chunk(
+                        h, self._chunk_steps(), _lib.ctypes.byref(t_out),
+                        _lib.ctypes.byref(rows)))
+                    if rows.value:
+                        tt = np.empty(rows.value)
+                        be.check(lib.mkg_read_log(h, _lib.dptr(tt), None,
+                                                  None, rows.value))
+                        times.append(tt)
+                    kms = _lib.ctypes.c_double()
+                    ncs = _lib.ctypes.c_int64()
+                    lib.mkg_last_stats(h, _lib.ctypes.byref(kms), None,
+                                       _lib.ctypes.byref(ncs))
+                    ms += kms.value
+                    cs += ncs.value
+            finally:
+                lib.mkg_set_frame_buffer(h, None, 0)
+            st = np.empty(self._nstate * self._ntotal)
+            be.check(lib.mkg_get_state(h, _lib.dptr(st), st.size))
+            self._state = st
+            self._last_stats = {'kernel_ms': ms, 'cell_steps': cs,
+                                'launches': None, 'all_launches': None}
+        self._time += duration
+        t = np.concatenate(times) if times else np.zeros(0)
+        shape = (len(t), self._ny, self._nx) if len(self._dims) == 2 else (
+            len(t), self._nx)
+        return t, frames[:len(t)].reshape(shape)
+
     def cuda_stream(self):
         """
         The CUDA stream (an integer handle) the last run was queued on, or

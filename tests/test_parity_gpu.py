@@ -356,3 +356,26 @@ def test_autotune_keeps_results(br77, tmp_path, monkeypatch):
     assert c._tuned_choice() is not None
     c.run(2)
     assert np.array_equal(a, c.state_array())
+
+
+def test_run_frames_equal_logged_values(decker):
+    # Frames kept on the device equal the values a normal log records
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    out = []
+    for frames in (True, False):
+        s = mg.SimulationCUDA(decker, p, ncells=(40, 24), rl=True)
+        s.set_paced_cells(3, 24)
+        if frames:
+            t, f = s.run_frames(6, 1.5)
+            out.append((np.asarray(t), f.cpu().numpy(), s.state_array()))
+        else:
+            keys = ['%d.%d.membrane.V' % (x, y) for y in range(24)
+                    for x in range(40)]
+            d = s.run(6, log=['engine.time'] + keys, log_interval=1.5)
+            v = np.stack([np.asarray(d[k]) for k in keys], axis=1)
+            out.append((np.asarray(d['engine.time']),
+                        v.reshape(-1, 24, 40), s.state_array()))
+    assert len(out[0][0]) == 4
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2])
