@@ -72,6 +72,16 @@ def parse():
     p.add_argument('--c5-full', action='store_true',
                    help='run the whole 1000 ms S1-S2 protocol of the'
                         ' 2048x2048 sheet instead of a 20 ms window')
+    p.add_argument('--profile', action='store_true',
+                   help='run one small sheet case for a profiler and exit')
+    p.add_argument('--profile-steps', type=int, default=40)
+    p.add_argument('--no-stage', action='store_true',
+                   help='profile the kernel that reads tiles from global'
+                        ' memory instead of staging them with TMA')
+    p.add_argument('--precision', choices=['single', 'double'],
+                   default='single')
+    p.add_argument('--accumulate', choices=['none', 'kahan', 'double'],
+                   default='none')
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-seconds', type=float, default=12.0,
                    help='target CPU work for the cpu_baseline sample')
@@ -540,7 +550,55 @@ def config_c5(args, device):
     out['value'] = n * n * steps / (ms / 1000)
     out['e2e'] = n * n * steps / wall
     out['unit'] = UNIT
+    k = s._last_kernel
+    peak, kind = read_peaks()
+    bpcs = k.bytes_per_cell_step()
+    out['roofline'] = {'bound': 'hbm', 'bytes_per_cell_step': bpcs,
+                       'achieved': out['value'] * bpcs / 1e9, 'peak': peak,
+                       'unit': 'GB/s', 'peak_source': kind,
+                       'frac': out['value'] * bpcs / 1e9 / peak}
+    del s, frames
+    torch.cuda.empty_cache()
+
+    # The plain FP64 path on the same sheet, over 1 ms (200 steps)
+    s64 = mg.SimulationCUDA(m, s1, ncells=(n, n), rl=True, device=device,
+                            precision=myokit.DOUBLE_PRECISION)
+    s64.set_step_size(0.005)
+    s64.set_paced_cells(nx=4, ny=n, x=0, y=0)
+    s64.run(0.05, log=['engine.time'], log_interval=1)
+    s64.run(1, log=['engine.time'], log_interval=1)
+    st = s64.last_run_stats()
+    v64 = st['cell_steps'] / (st['kernel_ms'] / 1000)
+    out['fp64'] = {'value': v64, 'unit': UNIT, 'window_ms': 1}
+    out['speedup_over_fp64'] = out['value'] / v64
     return out
+
+
+def profile_case(args):
+    """
+    Runs the benchmark sheet (--size, --precision, --accumulate) for
+    --profile-steps time steps after a short warm-up, for profilers; prints
+    one line of launch statistics.
+    """
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+    prec = myokit.DOUBLE_PRECISION if args.precision == 'double' \
+        else myokit.SINGLE_PRECISION
+    acc = None if args.accumulate == 'none' else args.accumulate
+    s, log = make_sheet(mg.SimulationCUDA, prec, args.size,
+                        steps_per_launch=args.profile_steps, accumulate=acc,
+                        stage_tiles=not args.no_stage)
+    ms = args.profile_steps * 0.005
+    for _ in range(2):
+        s.run(ms, log=log, log_interval=1)
+    st = s.last_run_stats()
+    print(json.dumps({'size': args.size, 'precision': args.precision,
+                      'accumulate': args.accumulate,
+                      'staged': s._last_kernel.layout is not None,
+                      'steps': st['cell_steps']
+                      // (args.size * args.size), 'launches': st['launches'],
+                      'kernel_ms': st['kernel_ms']}))
+    return 0
 
 
 def run_reference(args):
@@ -788,6 +846,8 @@ def main():
     args = parse()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.profile:
+        return profile_case(args)
     return run_ours(args)
 
 

@@ -82,7 +82,22 @@ typedef struct mkg_config {
                                states stored and updated in FP64, 2 selected
                                states carry an FP32 Kahan compensation term */
     int32_t n_hi;           /* number of selected states (mkg_set_hi_states) */
+    int32_t stage;          /* 1: the kernel copies each warp tile's inputs
+                               into shared memory with TMA tensor copies and
+                               takes the tensor maps as a second parameter */
+    int32_t v_double;       /* 1: V is stored and updated in FP64 (hi_mode 1
+                               with V among the selected states) */
 } mkg_config;
+
+/*
+ * Shared-memory layout of a staged warp tile for this configuration, as the
+ * library lays out its tensor copies: out[0] tile width (cells), out[1]
+ * first staged state plane, out[2] staged state planes, out[3] staged V
+ * rows, out[4] 1 if 1D conductances are staged, out[5] bytes of shared
+ * memory per warp, out[6] bytes the copies of one tile deliver. All zero
+ * when cfg->stage is 0. Needs no GPU. No counterpart in the reference.
+ */
+int mkg_stage_layout(const mkg_config *cfg, int64_t *out);
 
 /*
  * Compiles generated CUDA C++ source to an sm_103a cubin with NVRTC.

@@ -51,11 +51,15 @@ class MkgConfig(ctypes.Structure):
         ('two_d', ctypes.c_int32),
         ('hi_mode', ctypes.c_int32),
         ('n_hi', ctypes.c_int32),
+        ('stage', ctypes.c_int32),
+        ('v_double', ctypes.c_int32),
     ]
 
 
 # Every symbol declared in include/mkg_tissue.h, with its signature
 SIGNATURES = {
+    'mkg_stage_layout': (ctypes.c_int, [
+        ctypes.POINTER(MkgConfig), ctypes.POINTER(ctypes.c_int64)]),
     'mkg_compile': (ctypes.c_int, [
         ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p),
         ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),

@@ -17,6 +17,8 @@
  * Also holds the fixed (not generated) kernels: AoS <-> SoA state
  * conversion and precision conversion of per-edge conductances.
  */
+#include <cuda.h>            /* CUtensorMap types; the driver entry point is
+                                looked up at run time */
 #include <cuda_runtime.h>
 #include <nvrtc.h>
 
@@ -139,6 +141,71 @@ int grid_for(long long n)
 }  // namespace
 
 /* ------------------------------------------------------------------------ */
+/* Warp-tile staging layout                                                 */
+/* ------------------------------------------------------------------------ */
+
+namespace {
+
+/* Shared-memory layout of one staged warp tile (per warp). The same rule is
+ * stated by stage_layout() in exporter.py, which writes it into the kernel;
+ * the kernel compares its tile byte count with mkg_launch.stage_tx and
+ * refuses to run on a mismatch. Tile inputs are copied from the tile's
+ * first cell (rounded down to 4 cells when 2D rows are not 4-cell aligned,
+ * width 36, else 32); V rows and 1D conductances start one cell earlier,
+ * rounded down alike, 40 wide. Every copy destination is 128-byte aligned:
+ * regions, and V rows within theirs, are padded to multiples of 128. */
+const int kStageVW = 40;
+
+struct StageLayout {
+    int sw = 0, lo = 0, np = 0, v_rows = 0, gx = 0;
+    int hsize = 0, vsize = 0;
+    int64_t v_row = 0;                  /* bytes between staged V rows */
+    int64_t off[5] = {0, 0, 0, 0, 0};   /* state, hi, field, v, gx */
+    int64_t bytes = 0, tx = 0;
+};
+
+void compute_stage_layout(const mkg_config *c, StageLayout *L)
+{
+    *L = StageLayout();
+    if (!c->stage) return;
+    const int real = c->real_bytes;
+    const bool grid = c->diffusion == MKG_DIFF_GRID ||
+                      c->diffusion == MKG_DIFF_HETERO;
+    const bool two_d = c->two_d && grid;
+    L->sw = (two_d && c->nx % 4 != 0) ? 36 : 32;
+    int lo = 0, hi = c->n_state;
+    if (c->diffusion != MKG_DIFF_NONE && c->i_vm >= 0) {
+        if (c->i_vm == 0) lo = 1;
+        if (c->i_vm == c->n_state - 1) hi = c->n_state - 1;
+    }
+    L->lo = lo;
+    L->np = std::max(0, hi - lo);
+    L->v_rows = grid ? (two_d ? 3 : 1) : 0;
+    L->gx = (c->diffusion == MKG_DIFF_HETERO && !two_d) ? 1 : 0;
+    L->hsize = c->hi_mode == MKG_HI_DOUBLE ? 8 : real;
+    L->vsize = c->v_double ? 8 : real;
+    const int64_t size[5] = {
+        (int64_t)L->np * L->sw * real,
+        (int64_t)c->n_hi * L->sw * L->hsize,
+        (int64_t)c->n_field * L->sw * real,
+        (int64_t)L->v_rows * kStageVW * L->vsize,
+        L->gx ? (int64_t)kStageVW * real : 0,
+    };
+    L->v_row = ((int64_t)kStageVW * L->vsize + 127) / 128 * 128;
+    int64_t off = 0, tx = 0;
+    for (int i = 0; i < 5; ++i) {
+        L->off[i] = off;
+        const int64_t room = i == 3 ? L->v_rows * L->v_row : size[i];
+        off += (room + 127) / 128 * 128;
+        tx += size[i];
+    }
+    L->bytes = off;
+    L->tx = tx;
+}
+
+}  // namespace
+
+/* ------------------------------------------------------------------------ */
 /* Simulation handle                                                        */
 /* ------------------------------------------------------------------------ */
 
@@ -174,6 +241,12 @@ struct mkg_sim {
     int v_double = 0;            /* V plane holds doubles */
     int vbytes = 4;              /* bytes per V plane entry */
     size_t stage_bytes = 0;
+
+    /* Warp-tile staging (cfg.stage): layout, dynamic shared memory per CTA
+     * and the tensor maps passed to the kernel */
+    StageLayout lay;
+    size_t tile_smem = 0;
+    mkg_tmaps tmaps;
 
     /* pinned host buffers */
     mkg_step *h_steps = nullptr;
@@ -458,6 +531,91 @@ void fill_launch(mkg_sim *s, mkg_launch *a)
     }
 }
 
+/* cuTensorMapEncodeTiled, looked up once through the runtime (the library
+ * does not link the driver API) */
+typedef CUresult (*EncodeTiledFn)(
+    CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+    CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+    CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled_fn()
+{
+    static std::once_flag once;
+    static EncodeTiledFn fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p,
+                                             12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    });
+    return fn;
+}
+
+/* A rank-1 (d1 == 0) or rank-2 tensor map of FP32 / FP64 elements over
+ * d0 x d1 elements, rows d0 elements apart, copied in boxes b0 x b1 */
+int encode_map(mkg_sim *s, mkg_tmap *out, const void *base, int elem,
+               uint64_t d0, uint64_t d1, uint32_t b0, uint32_t b1)
+{
+    static_assert(sizeof(CUtensorMap) == sizeof(mkg_tmap),
+                  "tensor map size");
+    EncodeTiledFn fn = encode_tiled_fn();
+    if (!fn)
+        return set_err(s, MKG_ERR_CUDA,
+                       "cuTensorMapEncodeTiled is not available");
+    if (!base) return set_err(s, MKG_ERR_ARG, "a staged array is missing");
+    CUtensorMap m;
+    const cuuint32_t rank = d1 ? 2 : 1;
+    const cuuint64_t dims[2] = {d0, d1 ? d1 : 1};
+    const cuuint64_t strides[1] = {d0 * (cuuint64_t)elem};
+    const cuuint32_t box[2] = {b0, b1 ? b1 : 1};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(
+        &m, elem == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                      : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+        rank, const_cast<void *>(base), dims, strides, box, estr,
+        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return set_err(s, MKG_ERR_CUDA, "tensor map encoding failed (%d)",
+                       (int)r);
+    memcpy(out, &m, sizeof(m));
+    return MKG_OK;
+}
+
+/* Tensor maps of every staged array, for the current buffers */
+int encode_stage_maps(mkg_sim *s)
+{
+    const StageLayout &L = s->lay;
+    const mkg_config &c = s->cfg;
+    memset(&s->tmaps, 0, sizeof(s->tmaps));
+    int r;
+    if (L.np > 0 &&
+        (r = encode_map(s, &s->tmaps.state, s->d_state, s->real, s->pitch,
+                        c.n_state, L.sw, L.np)))
+        return r;
+    if (c.n_hi > 0 &&
+        (r = encode_map(s, &s->tmaps.hi, s->d_hi, L.hsize, s->pitch, c.n_hi,
+                        L.sw, c.n_hi)))
+        return r;
+    if (c.n_field > 0 &&
+        (r = encode_map(s, &s->tmaps.field, s->d_field, s->real, s->pitch,
+                        c.n_field, L.sw, c.n_field)))
+        return r;
+    if (L.v_rows > 0 &&
+        (r = encode_map(s, &s->tmaps.v, s->d_vbuf, L.vsize, s->pitch, 2,
+                        kStageVW, 1)))
+        return r;
+    if (L.gx &&
+        (r = encode_map(s, &s->tmaps.gx, s->d_gx, s->real,
+                        std::max<int64_t>(s->ncell - 1, 1), 0, kStageVW, 0)))
+        return r;
+    return MKG_OK;
+}
+
 /* CTAs needed to give every warp tile a warp */
 long long blocks_needed(const mkg_sim *s, const mkg_launch *a)
 {
@@ -609,6 +767,17 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
                        "the CTA must be (32*k, 1) threads");
     if (!cfg->two_d && cfg->ny != 1 && cfg->diffusion != MKG_DIFF_NONE)
         return set_err(nullptr, MKG_ERR_ARG, "2D diffusion needs two_d");
+    if (cfg->v_double && cfg->hi_mode != MKG_HI_DOUBLE)
+        return set_err(nullptr, MKG_ERR_ARG, "v_double needs hi_mode 1");
+    if (cfg->stage) {
+        /* Tensor copy limits: 256 planes per box, int32 coordinates */
+        StageLayout L;
+        compute_stage_layout(cfg, &L);
+        if (L.np > 256 || cfg->n_hi > 256 || cfg->n_field > 256 ||
+            cfg->nx * cfg->ny + 64 > (int64_t)INT_MAX)
+            return set_err(nullptr, MKG_ERR_ARG,
+                           "this configuration cannot stage tiles");
+    }
 
     mkg_sim *s = new mkg_sim();
     s->cfg = *cfg;
@@ -636,9 +805,17 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
     CKC(cudaLibraryGetKernel(&s->kernel, s->lib, "mkg_tissue_step"));
     CKC(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount,
                                cfg->device));
+    if (cfg->stage) {
+        compute_stage_layout(cfg, &s->lay);
+        /* + 128: the kernel rounds the base up to a 128-byte boundary */
+        s->tile_smem = (size_t)(cfg->block_x / 32) * s->lay.bytes + 128;
+        CKC(cudaKernelSetAttributeForDevice(
+            s->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            (int)s->tile_smem, cfg->device));
+    }
     CKC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &s->occ_blocks, (const void *)s->kernel,
-        cfg->block_x * cfg->block_y, 0));
+        cfg->block_x * cfg->block_y, s->tile_smem));
     if (s->occ_blocks < 1) {
         set_err(nullptr, MKG_ERR_CUDA,
                 "the generated kernel cannot be resident on an SM");
@@ -694,6 +871,9 @@ int mkg_set_hi_states(mkg_sim *s, const int32_t *states, int32_t n)
     s->v_double = (s->cfg.hi_mode == MKG_HI_DOUBLE && diffusion_on(s) &&
                    slot[s->cfg.i_vm] >= 0) ? 1 : 0;
     s->vbytes = s->v_double ? 8 : s->real;
+    if (s->cfg.stage && s->v_double != s->cfg.v_double)
+        return set_err(s, MKG_ERR_ARG,
+                       "the accumulated states disagree with v_double");
     return MKG_OK;
 }
 
@@ -1056,6 +1236,11 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
     if (s->frame_buf)
         a.log = (char *)s->frame_buf +
                 (size_t)s->frame_next * s->log_ncol * s->real;
+    if (s->cfg.stage) {
+        r = encode_stage_maps(s);
+        if (r) return r;
+        a.stage_tx = (int)s->lay.tx;
+    }
     const int threads = bx * by;
     const long long nblocks = blocks_needed(s, &a);
     int bpsm = s->blocks_per_sm > 0 ? std::min(s->blocks_per_sm, s->occ_blocks)
@@ -1102,7 +1287,7 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
             a.step0 = (int)off;
             a.epoch_base = epoch;
             a.v_sel = diffusion_on(s) ? (v_sel0 ^ (int)(off & 1)) : 0;
-            void *args[] = {&a};
+            void *args[] = {&a, &s->tmaps};
             cudaLaunchConfig_t lc;
             memset(&lc, 0, sizeof(lc));
             cudaLaunchAttribute attr[1];
@@ -1120,7 +1305,7 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
                 grid = std::min<long long>(nblocks, 1 << 30);
             }
             lc.gridDim = dim3((unsigned)grid, 1, 1);
-            lc.dynamicSmemBytes = 0;
+            lc.dynamicSmemBytes = s->tile_smem;
             const cudaError_t e = cudaLaunchKernelExC(
                 &lc, (const void *)s->kernel, args);
             if (e != cudaSuccess) {
@@ -1230,6 +1415,16 @@ int mkg_last_stats(const mkg_sim *s, double *kernel_ms, int64_t *launches,
     if (kernel_ms) *kernel_ms = s->last_ms;
     if (launches) *launches = s->last_launches;
     if (cell_steps) *cell_steps = s->last_cell_steps;
+    return MKG_OK;
+}
+
+int mkg_stage_layout(const mkg_config *cfg, int64_t *out)
+{
+    if (!cfg || !out) return set_err(nullptr, MKG_ERR_ARG, "null argument");
+    StageLayout L;
+    compute_stage_layout(cfg, &L);
+    const int64_t v[7] = {L.sw, L.lo, L.np, L.v_rows, L.gx, L.bytes, L.tx};
+    memcpy(out, v, sizeof(v));
     return MKG_OK;
 }
 

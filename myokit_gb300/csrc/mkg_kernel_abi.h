@@ -2,7 +2,8 @@
  * mkg_kernel_abi.h -- argument block shared by the host library and the
  * generated tissue kernels. Included by mkg_host.cu and prepended (as text)
  * to every generated kernel compiled with NVRTC, so both sides agree on the
- * layout. Plain C types only: NVRTC compiles it without system headers.
+ * layout. Plain C types only (and C++11 alignas): NVRTC compiles it
+ * without system headers.
  */
 #ifndef MKG_KERNEL_ABI_H
 #define MKG_KERNEL_ABI_H
@@ -10,6 +11,8 @@
 /* Device error codes written to mkg_status.error */
 #define MKG_DEV_OK        0
 #define MKG_DEV_TIMEOUT   1   /* grid barrier wait exceeded timeout_ns */
+#define MKG_DEV_STAGE     2   /* tile staging: the host's layout differs from
+                                 the kernel's, or a copy wait timed out */
 
 #define MKG_NO_HALT 0x7fffffff
 
@@ -62,7 +65,9 @@ typedef struct mkg_launch {
     int n_log_items;
     int nan_check;           /* apply the NaN halt at log rows */
     int ntiles_x, ntiles_y;  /* warp tiles (32 cells) per row, and rows */
-    int stage_tiles;         /* reserved */
+    int stage_tx;            /* bytes the tensor copies of one staged tile
+                                deliver, as the host laid them out; 0 when
+                                the kernel does not stage tiles */
     int step0;               /* index of this launch's first step within
                                 the chunk (for the NaN halt) */
     int epoch_base;          /* grid barriers completed by earlier launches
@@ -75,6 +80,21 @@ typedef struct mkg_launch {
     void *traj;              /* adjoint forward pass only: the states at t
                                 of every step, Real[nsteps][n_state][pitch] */
 } mkg_launch;
+
+/* An opaque TMA tensor map (CUtensorMap: 128 bytes, 64-byte aligned) */
+typedef struct mkg_tmap {
+    alignas(64) unsigned long long m[16];
+} mkg_tmap;
+
+/* Tensor maps of the arrays a staging kernel copies per warp tile; passed
+ * as a second, __grid_constant__ kernel parameter. */
+typedef struct mkg_tmaps {
+    mkg_tmap state;          /* Real[n_state][pitch] */
+    mkg_tmap hi;             /* accumulation planes [n_hi][pitch] */
+    mkg_tmap field;          /* Real[n_field][pitch] */
+    mkg_tmap v;              /* VReal[2][pitch] */
+    mkg_tmap gx;             /* Real[nx - 1]: 1D heterogeneous conductances */
+} mkg_tmaps;
 
 /* Arguments of the adjoint kernel: one checkpoint segment in reverse. */
 typedef struct mkg_adj_launch {

@@ -262,6 +262,62 @@ def _read(name):
         return f.read()
 
 
+# Shared-memory staging of warp-tile inputs with TMA (tensor copies). The
+# same rule is restated by stage_layout() in csrc/mkg_host.cu, which builds
+# the tensor maps and sizes the dynamic shared memory; the kernel refuses
+# to run when the two disagree on the bytes per tile.
+STAGE_VW = 40            # staged V / conductance row: 32 cells + halo + pad
+STAGE_MAX_BOX = 256      # planes per tensor copy
+STAGE_MAX_CTA = 200 * 1024
+
+
+def stage_layout(real_bytes, n_state, i_vm, n_field, n_hi, hi_bytes, v_bytes,
+                 v_rows, gx, row_pad):
+    """
+    Per-warp shared-memory layout of one staged warp tile. Tile inputs are
+    copied from x = the tile's first cell, rounded down to a multiple of 4
+    cells when rows are not 4-cell aligned (``row_pad``; the copy is then
+    36 cells wide, else 32), so that every copy starts on a 16-byte
+    boundary. V rows (and 1D conductances) start one cell earlier, rounded
+    down the same way, and are 40 wide. Every copy lands on a 128-byte
+    aligned address: regions, and each V row within its region
+    (``v_row_bytes`` apart), are padded to multiples of 128 bytes.
+
+    Returns a dict with the tile width ``sw``, the first staged state plane
+    ``lo`` and count ``np`` (the membrane potential plane is skipped when it
+    is the first or last state), region offsets, ``bytes`` per warp and
+    ``tx``, the bytes the copies of one tile deliver.
+    """
+    sw = 36 if row_pad else 32
+    v_row = (STAGE_VW * v_bytes + 127) // 128 * 128
+    lo, hi = 0, n_state
+    if i_vm >= 0:
+        if i_vm == 0:
+            lo = 1
+        if i_vm == n_state - 1:
+            hi = n_state - 1
+    npl = max(0, hi - lo)
+    sizes = [
+        ('state', npl * sw * real_bytes),
+        ('hi', n_hi * sw * hi_bytes),
+        ('field', n_field * sw * real_bytes),
+        ('v', v_rows * STAGE_VW * v_bytes),
+        ('gx', STAGE_VW * real_bytes if gx else 0),
+    ]
+    out = {'sw': sw, 'vw': STAGE_VW, 'lo': lo, 'np': npl, 'v_rows': v_rows,
+           'gx': 1 if gx else 0, 'v_row_bytes': v_row}
+    off = 0
+    tx = 0
+    for name, n in sizes:
+        out[name + '_off'] = off
+        room = v_rows * v_row if name == 'v' else n
+        off += (room + 127) // 128 * 128
+        tx += n
+    out['bytes'] = off
+    out['tx'] = tx
+    return out
+
+
 class TissueKernel(object):
     """
     The generated CUDA source for one simulation configuration, with the
@@ -298,11 +354,19 @@ class TissueKernel(object):
         (correctly rounded division), or ``'fast'`` (reciprocal
         multiplication for constant denominators, the hardware reciprocal
         elsewhere, denormals flushed to zero).
+    ``stage``
+        Copy each warp tile's states, accumulation planes, fields and V
+        rows into shared memory with TMA tensor copies, one tile ahead of
+        the computation (ignored when the layout does not fit).
+    ``row_pad``
+        Rows of the grid are not a multiple of 4 cells (2D only): staged
+        copies are then 36 cells wide.
     """
     def __init__(self, model, precision, native_math, bound_variables,
                  inter_log, diffusion, two_d, fields, rl_states, block,
                  fast_divide=True, min_blocks=1, math='default',
-                 accumulate=None, accumulate_states=(), traj=False):
+                 accumulate=None, accumulate_states=(), traj=False,
+                 stage=False, row_pad=False):
         self.model = model
         self.single = (precision == myokit.SINGLE_PRECISION)
         self.native_math = bool(native_math)
@@ -341,6 +405,23 @@ class TissueKernel(object):
         self.v_double = (self.accumulate == 'double' and
                          self.i_vm in self.hi_index)
         self.traj = bool(traj)
+        self.layout = None
+        if stage and not self.traj:
+            real = 4 if self.single else 8
+            v_rows = 0
+            if self.diffusion in (DIFF_GRID, DIFF_HETERO):
+                v_rows = 3 if self.two_d else 1
+            lay = stage_layout(
+                real, self.n_state, self.i_vm, len(self.fields),
+                len(self.hi_states),
+                8 if self.accumulate == 'double' else real,
+                8 if self.v_double else real, v_rows,
+                self.diffusion == DIFF_HETERO and not self.two_d,
+                bool(row_pad) and self.two_d)
+            if (max(lay['np'], len(self.hi_states), len(self.fields))
+                    <= STAGE_MAX_BOX and
+                    lay['bytes'] * (self.block[0] // 32) <= STAGE_MAX_CTA):
+                self.layout = lay
         self.census = OpCensus()
         self._source = self._generate()
 
@@ -432,11 +513,16 @@ class TissueKernel(object):
         self.literal_subst = literal_subst
         self.cell_const_eqs = []
         self.rhs_eqs = []
-        body.append(tab + '// Per-cell constants (scalar fields)')
+        # Scalar fields are read with the states (below); constants that
+        # depend on them are computed per cell here.
+        lay = self.layout
+        sw = lay['sw'] if lay else 0
+        field_loads = []
         for k, var in enumerate(self.fields):
-            body.append(
-                f'{tab}const Real {self._name(var)} = '
-                f'field[(long long){k} * pitch + cid];')
+            src = (f's_fd[{k * sw}]' if lay else
+                   f'field[(long long){k} * pitch + cid]')
+            field_loads.append(f'{tab}const Real {self._name(var)} = {src};')
+        body.append(tab + '// Per-cell constants (scalar fields)')
         for eq in const_eqs:
             var = eq.lhs.var()
             if var in percell_const and var not in field_set:
@@ -466,15 +552,24 @@ class TissueKernel(object):
             plane = f'(long long){i} * pitch + cid'
             if j is not None:
                 hplane = f'(long long){j} * pitch + cid'
+            if lay:
+                # Staged in shared memory (see stage_layout)
+                src = f's_st[{(i - lay["lo"]) * sw}]'
+                hsrc = f's_hi[{j * sw}]' if j is not None else None
+            else:
+                src = f'state[{plane}]'
+                hsrc = None
             if i == self.i_vm:
                 loads.append(f'{tab}const Real {n} = (Real)V_;')
             elif j is not None and self.accumulate == 'double':
-                loads.append(f'{tab}const double X{n} = {hiD}[{hplane}];')
+                loads.append(
+                    f'{tab}const double X{n} = {hsrc or hiD + "[" + hplane + "]"};')
                 loads.append(f'{tab}const Real {n} = (Real)X{n};')
             else:
-                loads.append(f'{tab}const Real {n} = state[{plane}];')
+                loads.append(f'{tab}const Real {n} = {src};')
             if j is not None and self.accumulate == 'kahan':
-                loads.append(f'{tab}const Real C{n} = {hiR}[{hplane}];')
+                loads.append(
+                    f'{tab}const Real C{n} = {hsrc or hiR + "[" + hplane + "]"};')
             target = 'vout[cid]' if i == self.i_vm else f'state[{plane}]'
             if s in self.rl_states:
                 inf, tau = self.rl_states[s]
@@ -584,11 +679,32 @@ class TissueKernel(object):
             '@BY@': str(self.block[1]),
             '@MINB@': str(self.min_blocks),
             '@POW_HELPERS@': _pow_helpers(self.single),
-            '@LOADS@': '\n'.join(loads),
+            '@LOADS@': '\n'.join(loads + field_loads),
             '@LOG_A@': log_a,
             '@BODY@': '\n'.join(body),
             '@LOG_B@': log_b,
         }
+        lay = self.layout or {}
+        subs.update({
+            '@STAGE@': '1' if self.layout else '0',
+            '@SW@': str(lay.get('sw', 32)),
+            '@VW@': str(STAGE_VW),
+            '@ST_LO@': str(lay.get('lo', 0)),
+            '@ST_NP@': str(lay.get('np', 0)),
+            '@HI_NP@': str(len(self.hi_states) if lay else 0),
+            '@FD_NP@': str(len(self.fields) if lay else 0),
+            '@V_ROWS@': str(lay.get('v_rows', 0)),
+            '@GX_STAGE@': str(lay.get('gx', 0)),
+            '@ST_OFF@': str(lay.get('state_off', 0)),
+            '@HI_OFF@': str(lay.get('hi_off', 0)),
+            '@FD_OFF@': str(lay.get('field_off', 0)),
+            '@V_OFF@': str(lay.get('v_off', 0)),
+            '@GX_OFF@': str(lay.get('gx_off', 0)),
+            '@V_ROW_BYTES@': str(lay.get('v_row_bytes', 0)),
+            '@STAGE_BYTES@': str(lay.get('bytes', 0)),
+            '@TX_BYTES@': str(lay.get('tx', 0)),
+            '@HREAL@': 'double' if self.accumulate == 'double' else real,
+        })
         text = _read('tissue_kernel.cu.in')
         for k, v in subs.items():
             text = text.replace(k, v)

@@ -135,6 +135,10 @@ class SimulationCUDA(object):
         The states to accumulate; by default the membrane potential, states
         with concentration units and non-gating states of magnitude >= 1,
         whose per-step increments are smallest relative to their value.
+    ``stage_tiles``
+        Copy each warp tile's states, fields and V rows into shared memory
+        with TMA tensor copies, one tile ahead of the computation (grids of
+        256 cells or more). Results are identical either way.
     """
     _index = 0
 
@@ -142,7 +146,8 @@ class SimulationCUDA(object):
             self, model, protocol=None, ncells=256, diffusion=True,
             precision=myokit.SINGLE_PRECISION, native_maths=False, rl=False,
             block=None, steps_per_launch=0, device=0, min_blocks=None,
-            fp32_math='fast', accumulate=None, accumulate_states=None):
+            fp32_math='fast', accumulate=None, accumulate_states=None,
+            stage_tiles=True):
 
         # Model checks (openclsim.py:155-167)
         if not model.is_valid():
@@ -245,6 +250,7 @@ class SimulationCUDA(object):
         self._block = block
         self._min_blocks = min_blocks
         self._fp32_math = fp32_math
+        self._stage_tiles = bool(stage_tiles)
         if accumulate not in (None, 'double', 'kahan'):
             raise ValueError(
                 'The argument "accumulate" must be None, "double" or'
@@ -828,10 +834,14 @@ class SimulationCUDA(object):
         block = self._block_shape(two_d)
         minb = self._default_min_blocks(block)
         acc = self.accumulated_states()
+        # Tile staging with TMA for grids of at least 256 cells; rows that
+        # are not a multiple of 4 cells need the padded copy width
+        stage = self._stage_tiles and self._ntotal >= 256
+        row_pad = two_d and self._nx % 4 != 0
         key = (
             self._model_version, self._precision, self._native_math, mode,
             two_d, block, minb, self._fp32_math, self._accumulate,
-            tuple(v.qname() for v in acc),
+            stage, row_pad, tuple(v.qname() for v in acc),
             tuple(v.qname() for v in self._fields.keys()),
             tuple(v.qname() for v in inter_log))
         k = self._kernels.get(key)
@@ -841,7 +851,8 @@ class SimulationCUDA(object):
                 self._bound_variables, inter_log, mode, two_d,
                 list(self._fields.keys()), self._rl_states, block,
                 min_blocks=minb, math=self._fp32_math,
-                accumulate=self._accumulate, accumulate_states=acc)
+                accumulate=self._accumulate, accumulate_states=acc,
+                stage=stage, row_pad=row_pad)
             if len(self._kernels) > 16:
                 self._kernels.clear()
             self._kernels[key] = k
@@ -865,6 +876,8 @@ class SimulationCUDA(object):
         cfg.hi_mode = {None: 0, 'double': 1, 'kahan': 2}[kernel.accumulate] \
             if kernel.hi_states else 0
         cfg.n_hi = len(kernel.hi_states)
+        cfg.stage = 1 if kernel.layout else 0
+        cfg.v_double = 1 if kernel.v_double else 0
         key = (kernel.key(), bytes(cfg))
         if self._backend is not None and self._backend[0] == key:
             return self._backend[1]
