@@ -19,12 +19,16 @@ import numpy as np
 from ._deps import myokit
 
 # Candidate (threads per CTA, min CTAs per SM, steps per launch); the
-# register cap is 64K / (threads * min CTAs)
+# register cap is 64K / (threads * min CTAs). 576 and 640 threads trade
+# registers for the 18 or 20 warps per SM that even out the warp tiles of
+# mid-size sheets.
 _CANDIDATES = [
     ((256, 1), 2, 0), ((128, 1), 4, 0), ((512, 1), 1, 0), ((192, 1), 3, 0),
-    ((384, 1), 1, 0), ((128, 1), 1, 0), ((256, 1), 2, 1), ((128, 1), 4, 1),
+    ((384, 1), 1, 0), ((576, 1), 1, 0), ((640, 1), 1, 0), ((128, 1), 1, 0),
+    ((256, 1), 2, 1), ((128, 1), 4, 1),
 ]
-_CANDIDATES_FP64 = [((128, 1), 1, 0), ((256, 1), 1, 0), ((64, 1), 1, 0)]
+_CANDIDATES_FP64 = [((128, 1), 1, 0), ((256, 1), 1, 0), ((64, 1), 1, 0),
+                    ((32, 1), 1, 0)]
 
 
 def _cache_path():
@@ -45,7 +49,8 @@ def signature(sim):
         sim._model.name(), code, sim._nx, sim._ny, len(sim._dims),
         sim._precision, sim._accumulate, sim._diffusion_mode(),
         ','.join(v.qname() for v in sim._fields), len(sim._rl_states),
-        sim._fp32_math, sim._native_math))
+        sim._fp32_math, sim._native_math,
+        'staged' if sim._stage_tiles else 'direct'))
 
 
 def _load(path):
