@@ -67,14 +67,24 @@ def parse():
                    help='simulated time of the adjoint measurement'
                         ' (0 = skip)')
     p.add_argument('--configs', default='c1,c3,c5',
-                   help='other BASELINE configurations to time (comma list'
-                        ' of c1, c3, c5; empty = none)')
+                   help='other configurations to time: comma list of c1'
+                        ' (200-cell FP64 cable), c3 (512 batched cables), c5'
+                        ' (2048x2048 S1-S2 sheet), or none')
     p.add_argument('--c5-full', action='store_true',
                    help='run the whole 1000 ms S1-S2 protocol of the'
                         ' 2048x2048 sheet instead of a 20 ms window')
     p.add_argument('--profile', action='store_true',
                    help='run one small sheet case for a profiler and exit')
     p.add_argument('--profile-steps', type=int, default=40)
+    p.add_argument('--profile-adjoint', action='store_true',
+                   help='with --profile: run the discrete adjoint (loss on'
+                        ' 64 probes, checkpoints every 200 steps) instead')
+    p.add_argument('--adj-min-blocks', type=int, default=1,
+                   help='resident CTAs per SM asked for the reverse kernel')
+    p.add_argument('--adj-threads', type=int, default=0,
+                   help='CTA size of the reverse kernel (0: the forward\'s)')
+    p.add_argument('--adj-no-guards', action='store_true',
+                   help='straight-line reverse sweep')
     p.add_argument('--no-stage', action='store_true',
                    help='profile the kernel that reads tiles from global'
                         ' memory instead of staging them with TMA')
@@ -585,6 +595,36 @@ def profile_case(args):
     prec = myokit.DOUBLE_PRECISION if args.precision == 'double' \
         else myokit.SINGLE_PRECISION
     acc = None if args.accumulate == 'none' else args.accumulate
+    if args.profile_adjoint:
+        from myokit_gb300 import adjoint as ad
+        s, _ = make_sheet(mg.SimulationCUDA, prec, args.size,
+                          stage_tiles=not args.no_stage)
+        rng = np.random.default_rng(5)
+        cells = rng.choice(args.size ** 2, 64, replace=False)
+        probes = [(int(c % args.size), int(c // args.size)) for c in cells]
+        adj = ad.TissueAdjoint(s, probes, segment_steps=200,
+                               min_blocks=args.adj_min_blocks,
+                               threads=args.adj_threads or None,
+                               guards=not args.adj_no_guards)
+        ms = args.profile_steps * 0.005
+        out = {}
+        for _ in range(2):
+            t0 = time.perf_counter()
+            v = adj.forward(ms, 0.05)
+            t1 = time.perf_counter()
+            adj.backward(2 * (v + 80))
+            t2 = time.perf_counter()
+            s.run(ms, log=['engine.time'], log_interval=0.05)
+            t3 = time.perf_counter()
+            out = {'adjoint_forward_s': t1 - t0, 'adjoint_backward_s': t2 - t1,
+                   'forward_s': t3 - t2,
+                   'ratio': (t2 - t0) / (t3 - t2)}
+        print(json.dumps(dict(out, size=args.size, steps=args.profile_steps,
+                              adj_min_blocks=args.adj_min_blocks,
+                              adj_threads=args.adj_threads,
+                              guards=not args.adj_no_guards,
+                              staged=s._last_kernel.layout is not None)))
+        return 0
     s, log = make_sheet(mg.SimulationCUDA, prec, args.size,
                         steps_per_launch=args.profile_steps, accumulate=acc,
                         stage_tiles=not args.no_stage)
@@ -792,7 +832,7 @@ def run_ours(args):
         adj = adjoint_runs(args, local)
 
     others = {}
-    wanted = [c for c in args.configs.split(',') if c]
+    wanted = [c for c in args.configs.split(',') if c and c != 'none']
     if rank == 0:
         for c in wanted:
             others[c] = {'c1': config_c1, 'c3': config_c3,

@@ -189,7 +189,7 @@ class AdjointKernel(object):
     Supports forward-Euler and Rush-Larsen updates, homogeneous grid
     diffusion (1D or 2D) or none, and scalar fields.
     """
-    def __init__(self, fwd):
+    def __init__(self, fwd, min_blocks=1, threads=None, guards=True):
         if fwd.diffusion not in (_exp.DIFF_NONE, _exp.DIFF_GRID):
             raise NotImplementedError(
                 'The adjoint supports homogeneous grid diffusion only.')
@@ -198,6 +198,11 @@ class AdjointKernel(object):
                 'The adjoint runs without accumulation modes.')
         self.fwd = fwd
         self.single = fwd.single
+        self.min_blocks = int(min_blocks)
+        self.threads = int(threads or fwd.block[0])
+        if self.threads % 32 or not 32 <= self.threads <= 1024:
+            raise ValueError('threads must be a multiple of 32 up to 1024')
+        self.guards = bool(guards)
         self._source = self._generate()
 
     def _generate(self):
@@ -282,7 +287,12 @@ class AdjointKernel(object):
                     continue
                 terms.append(f'{tab}    {A(rn)} += a_ * ({w.ex(dp)});')
             if terms:
-                rev.append(f'{tab}if ({a} != 0) {{ const Real a_ = {a};')
+                # With guards an equation whose adjoint is still zero is
+                # skipped; without, the sweep is straight-line code
+                if self.guards:
+                    rev.append(f'{tab}if ({a} != 0) {{ const Real a_ = {a};')
+                else:
+                    rev.append(f'{tab}{{ const Real a_ = {a};')
                 rev.extend(terms)
                 rev.append(f'{tab}}}')
         for lhs, rhs in reversed(fwd.cell_const_eqs):
@@ -323,6 +333,8 @@ class AdjointKernel(object):
             '@DIFF@': str(fwd.diffusion),
             '@TWO_D@': '1' if fwd.two_d else '0',
             '@BX@': str(fwd.block[0]),
+            '@ADJ_MINB@': str(self.min_blocks),
+            '@ADJ_BX@': str(self.threads),
             '@POW_HELPERS@': _exp._pow_helpers(self.single),
             '@FORWARD@': '\n'.join(fw),
             '@SEEDS@': '\n'.join(seeds),
@@ -371,15 +383,30 @@ class TissueAdjoint(object):
         Steps between checkpoints: the backward pass recomputes each segment
         from its checkpoint, so memory is one segment's trajectory plus one
         state per segment.
+    ``min_blocks``, ``threads``
+        Resident CTAs per SM asked of the compiler for the reverse kernel,
+        and its CTA size (default: the simulation's); the register cap is
+        64K / (threads * min_blocks).
+    ``guards``
+        Skip the reverse of equations whose adjoint is still zero (one
+        branch per equation). The default, straight-line code, lets the
+        compiler schedule across equations and keeps the reverse kernel
+        free of register spills; results are the same while the partial
+        derivatives are finite.
 
     The simulation's state and time are not changed by :meth:`forward`.
     """
-    def __init__(self, sim, probes, segment_steps=200):
+    def __init__(self, sim, probes, segment_steps=200, min_blocks=1,
+                 threads=None, guards=False):
         if sim._accumulate is not None:
             raise NotImplementedError(
                 'The adjoint runs without accumulation modes.')
         self.sim = sim
         self.segment_steps = int(segment_steps)
+        self.min_blocks = int(min_blocks)
+        self.threads = threads
+        self.guards = bool(guards)
+        self._generated = {}
         vm = sim._vm
         if vm is None:
             raise ValueError('The adjoint needs a membrane potential.')
@@ -409,13 +436,23 @@ class TissueAdjoint(object):
         sim = self.sim
         kernel = sim._kernel([])
         be = sim._get_backend(kernel)
-        fwd = _exp.TissueKernel(
-            sim._model, sim._precision, sim._native_math,
-            sim._bound_variables, [], kernel.diffusion, kernel.two_d,
-            list(sim._fields.keys()), sim._rl_states, kernel.block,
-            min_blocks=1, math=sim._fp32_math, traj=True)
-        ak = AdjointKernel(fwd)
-        key = (id(be), ak.key(), self.segment_steps)
+        # Generated once per forward kernel (the forward kernel's key covers
+        # the model version, precision, fields and launch shape)
+        akey = (kernel.key(), self.min_blocks, self.threads, self.guards)
+        ak = self._generated.get(akey)
+        if ak is None:
+            # The trajectory-writing forward kernel has the launch shape,
+            # register cap and tile staging of the simulation's own kernel
+            fwd = _exp.TissueKernel(
+                sim._model, sim._precision, sim._native_math,
+                sim._bound_variables, [], kernel.diffusion, kernel.two_d,
+                list(sim._fields.keys()), sim._rl_states, kernel.block,
+                min_blocks=kernel.min_blocks, math=sim._fp32_math,
+                traj=True, stage=kernel.stage, row_pad=kernel.row_pad)
+            ak = AdjointKernel(fwd, self.min_blocks, self.threads,
+                               self.guards)
+            self._generated = {akey: ak}
+        key = (id(be), akey, self.segment_steps)
         if self._attached != key:
             cubin = compile_kernel(ak)
             be.check(be.lib.mkg_adj_attach(be.h, cubin, len(cubin),

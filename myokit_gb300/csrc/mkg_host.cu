@@ -291,6 +291,7 @@ struct mkg_sim {
     cudaLibrary_t adj_lib = nullptr;
     cudaKernel_t adj_fwd = nullptr, adj_bwd = nullptr;
     int adj_occ_fwd = 1, adj_occ_bwd = 1;
+    int adj_bwd_threads = 0;              /* reverse kernel CTA size */
     int adj_seg = 0;                      /* steps per checkpoint segment */
     void *d_traj = nullptr, *d_lam = nullptr, *d_mu = nullptr;
     void *d_gfield = nullptr, *d_gg = nullptr, *d_lgrad = nullptr;
@@ -1627,10 +1628,21 @@ extern "C" int mkg_adj_attach(mkg_sim *s, const void *cubin, size_t size,
     CK(s, cudaLibraryGetKernel(&s->adj_bwd, s->adj_lib,
                                "mkg_tissue_adjoint"));
     const int threads = s->cfg.block_x * s->cfg.block_y;
+    /* The trajectory kernel stages tiles like the simulation's kernel */
+    if (s->cfg.stage)
+        CK(s, cudaKernelSetAttributeForDevice(
+                  s->adj_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                  (int)s->tile_smem, s->cfg.device));
     CK(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &s->adj_occ_fwd, (const void *)s->adj_fwd, threads, 0));
+        &s->adj_occ_fwd, (const void *)s->adj_fwd, threads, s->tile_smem));
+    /* The reverse kernel's CTA size is its launch bound */
+    cudaFuncAttributes fa;
+    CK(s, cudaFuncGetAttributes(&fa, (const void *)s->adj_bwd));
+    s->adj_bwd_threads = fa.maxThreadsPerBlock;
+    if (s->adj_bwd_threads < 32 || s->adj_bwd_threads % 32)
+        return set_err(s, MKG_ERR_ARG, "invalid reverse kernel CTA size");
     CK(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &s->adj_occ_bwd, (const void *)s->adj_bwd, threads, 0));
+        &s->adj_occ_bwd, (const void *)s->adj_bwd, s->adj_bwd_threads, 0));
     if (s->adj_occ_fwd < 1 || s->adj_occ_bwd < 1)
         return set_err(s, MKG_ERR_CUDA, "adjoint kernels cannot be resident");
     const size_t plane = (size_t)s->pitch * s->real;
@@ -1742,7 +1754,7 @@ __global__ void k_sum_planes(const Real *__restrict__ in, long long n,
 }
 
 int launch_coop(mkg_sim *s, cudaKernel_t k, void *arg, int occ,
-                long long need)
+                long long need, size_t smem = 0, int threads = 0)
 {
     cudaLaunchConfig_t lc;
     memset(&lc, 0, sizeof(lc));
@@ -1751,11 +1763,14 @@ int launch_coop(mkg_sim *s, cudaKernel_t k, void *arg, int occ,
     attr[0].val.cooperative = 1;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    lc.blockDim = dim3(s->cfg.block_x * s->cfg.block_y, 1, 1);
+    lc.blockDim = dim3(threads ? threads : s->cfg.block_x * s->cfg.block_y,
+                       1, 1);
     lc.gridDim = dim3((unsigned)std::min<long long>(
         need, (long long)occ * s->num_sms), 1, 1);
     lc.stream = s->stream;
-    void *args[] = {arg};
+    lc.dynamicSmemBytes = smem;
+    /* A staging kernel takes the tensor maps as a second parameter */
+    void *args[] = {arg, &s->tmaps};
     CK(s, cudaLaunchKernelExC(&lc, (const void *)k, args));
     s->n_launches++;
     return MKG_OK;
@@ -1792,21 +1807,45 @@ int adj_backward(mkg_sim *s, const double *lgrad, int64_t rows,
                           plane * std::max(s->cfg.n_field, 1), s->stream));
     CK(s, cudaMemsetAsync(s->d_gg, 0, plane * 2, s->stream));
     int mu_sel = 0;
-    std::vector<mkg_step> fsteps(s->adj_seg), bsteps(s->adj_seg);
+    /* The whole schedule on the device, once: the reverse kernel reads the
+     * logged rows, the trajectory kernel logs nothing */
+    const size_t total = s->adj_sched.size();
+    std::vector<mkg_step> fsteps(s->adj_sched);
+    for (mkg_step &st : fsteps) st.log_row = -1;
+    dfree(s->d_fsteps);
+    dfree(s->d_bsteps);
+    CK(s, cudaMalloc((void **)&s->d_fsteps,
+                     std::max<size_t>(total, 1) * sizeof(mkg_step)));
+    CK(s, cudaMalloc((void **)&s->d_bsteps,
+                     std::max<size_t>(total, 1) * sizeof(mkg_step)));
+    if (total) {
+        CK(s, cudaMemcpyAsync(s->d_fsteps, fsteps.data(),
+                              total * sizeof(mkg_step),
+                              cudaMemcpyHostToDevice, s->stream));
+        CK(s, cudaMemcpyAsync(s->d_bsteps, s->adj_sched.data(),
+                              total * sizeof(mkg_step),
+                              cudaMemcpyHostToDevice, s->stream));
+    }
     mkg_status init;
     init.barrier = 0;
     init.error = MKG_DEV_OK;
     init.halt_step = MKG_NO_HALT;
     init.timeout_block = -1;
+    if (s->cfg.stage) {
+        int r = encode_stage_maps(s);
+        if (r) return r;
+    }
+    /* Segments are queued without host synchronisation. The status word
+     * is set once; before each launch only its barrier counter restarts, so
+     * a device error stays recorded (every launch checks it first and
+     * returns) and is read once at the end. */
+    *s->h_status = init;
+    CK(s, cudaMemcpyAsync(s->d_status, s->h_status, sizeof(mkg_status),
+                          cudaMemcpyHostToDevice, s->stream));
     for (long long g = (long long)s->adj_seg_len.size() - 1; g >= 0; --g) {
         const long long n = s->adj_seg_len[g];
         if (n == 0) continue;
         const long long st0 = s->adj_seg_start[g];
-        for (long long i = 0; i < n; ++i) {
-            bsteps[i] = s->adj_sched[st0 + i];
-            fsteps[i] = bsteps[i];
-            fsteps[i].log_row = -1;
-        }
         /* Restore the segment's checkpoint */
         const char *ck = (const char *)s->adj_ckpt[g];
         const int vsel = s->adj_seg_vsel[g];
@@ -1815,33 +1854,27 @@ int adj_backward(mkg_sim *s, const double *lgrad, int64_t rows,
         CK(s, cudaMemcpyAsync((char *)s->d_vbuf + (size_t)vsel * plane,
                               ck + plane * s->cfg.n_state, plane,
                               cudaMemcpyDeviceToDevice, s->stream));
-        CK(s, cudaMemcpyAsync(s->d_fsteps, fsteps.data(),
-                              n * sizeof(mkg_step), cudaMemcpyHostToDevice,
-                              s->stream));
-        CK(s, cudaMemcpyAsync(s->d_bsteps, bsteps.data(),
-                              n * sizeof(mkg_step), cudaMemcpyHostToDevice,
-                              s->stream));
         /* Forward over the segment, recording the trajectory */
         mkg_launch a;
         fill_launch(s, &a);
         a.n_log_items = 0;
         a.log_ncol = 0;
         a.nan_check = 0;
-        a.steps = s->d_fsteps;
+        a.steps = s->d_fsteps + st0;
         a.nsteps = (int)n;
         a.v_sel = vsel;
         a.traj = s->d_traj;
-        *s->h_status = init;
-        CK(s, cudaMemcpyAsync(s->d_status, s->h_status, sizeof(mkg_status),
-                              cudaMemcpyHostToDevice, s->stream));
+        if (s->cfg.stage) a.stage_tx = (int)s->lay.tx;
+        CK(s, cudaMemsetAsync(&s->d_status->barrier, 0, sizeof(unsigned),
+                              s->stream));
         int r = launch_coop(s, s->adj_fwd, &a, s->adj_occ_fwd,
-                            blocks_needed(s, &a));
+                            blocks_needed(s, &a), s->tile_smem);
         if (r) return r;
         /* The segment in reverse */
         mkg_adj_launch b;
         memset(&b, 0, sizeof(b));
         b.f = a;
-        b.f.steps = s->d_bsteps;
+        b.f.steps = s->d_bsteps + st0;
         b.f.traj = nullptr;
         b.traj = s->d_traj;
         b.lam = s->d_lam;
@@ -1852,19 +1885,24 @@ int adj_backward(mkg_sim *s, const double *lgrad, int64_t rows,
         b.lgrad = s->d_lgrad;
         b.nprobe = ncol;
         b.mu_sel = mu_sel;
-        CK(s, cudaMemcpyAsync(s->d_status, s->h_status, sizeof(mkg_status),
-                              cudaMemcpyHostToDevice, s->stream));
-        r = launch_coop(s, s->adj_bwd, &b, s->adj_occ_bwd,
-                        blocks_needed(s, &a));
+        CK(s, cudaMemsetAsync(&s->d_status->barrier, 0, sizeof(unsigned),
+                              s->stream));
+        const long long bwd_blocks =
+            ((long long)a.ntiles_x * a.ntiles_y * 32 + s->adj_bwd_threads -
+             1) / s->adj_bwd_threads;
+        r = launch_coop(s, s->adj_bwd, &b, s->adj_occ_bwd, bwd_blocks, 0,
+                        s->adj_bwd_threads);
         if (r) return r;
         mu_sel ^= (int)(n & 1);
-        CK(s, cudaMemcpyAsync(s->h_status, s->d_status, sizeof(mkg_status),
-                              cudaMemcpyDeviceToHost, s->stream));
-        CK(s, cudaStreamSynchronize(s->stream));
-        if (s->h_status->error != MKG_DEV_OK)
-            return set_err(s, MKG_ERR_TIMEOUT,
-                           "device barrier wait timed out in the adjoint");
     }
+    CK(s, cudaMemcpyAsync(s->h_status, s->d_status, sizeof(mkg_status),
+                          cudaMemcpyDeviceToHost, s->stream));
+    CK(s, cudaStreamSynchronize(s->stream));
+    if (s->h_status->error != MKG_DEV_OK)
+        return set_err(s, MKG_ERR_TIMEOUT,
+                       s->h_status->error == MKG_DEV_STAGE
+                           ? "tile staging failed in the adjoint"
+                           : "device barrier wait timed out in the adjoint");
     /* Field gradients (AoS doubles) and the conductance gradients */
     if (grad_fields && s->cfg.n_field > 0) {
         int r = download_soa<Real>(s, grad_fields, s->cfg.n_field,

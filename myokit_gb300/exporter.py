@@ -405,8 +405,10 @@ class TissueKernel(object):
         self.v_double = (self.accumulate == 'double' and
                          self.i_vm in self.hi_index)
         self.traj = bool(traj)
+        self.stage = bool(stage)
+        self.row_pad = bool(row_pad) and self.two_d
         self.layout = None
-        if stage and not self.traj:
+        if self.stage:
             real = 4 if self.single else 8
             v_rows = 0
             if self.diffusion in (DIFF_GRID, DIFF_HETERO):

@@ -187,3 +187,20 @@ def test_torch_function_gradients(br77):
         ref['gx'] + ref['gy'])
     for t, n in zip(fields, adj.field_names()):
         np.testing.assert_allclose(t.grad.numpy(), ref[n], rtol=1e-12)
+
+
+@pytest.mark.gpu
+def test_guarded_and_straight_line_sweeps_agree(br77):
+    shape = (5, 6)
+    s = _sim(br77, DP, fields=_fields(br77, shape, 1))
+    target = np.zeros((24, len(PROBES))) - 80
+    out = []
+    for guards in (True, False):
+        adj = adjoint.TissueAdjoint(s, PROBES, segment_steps=50,
+                                    guards=guards)
+        out.append(adj.loss_and_gradient(12, target, 0.5))
+    assert out[0][0] == out[1][0]
+    for k in out[0][1]:
+        np.testing.assert_allclose(np.asarray(out[0][1][k]),
+                                   np.asarray(out[1][1][k]), rtol=1e-12,
+                                   atol=0)
