@@ -18,17 +18,23 @@ import numpy as np
 
 from ._deps import myokit
 
-# Candidate (threads per CTA, min CTAs per SM, steps per launch); the
-# register cap is 64K / (threads * min CTAs). 576 and 640 threads trade
-# registers for the 18 or 20 warps per SM that even out the warp tiles of
-# mid-size sheets.
+# Candidate (threads per CTA, min CTAs per SM, steps per launch, lazy tile
+# staging); the register cap is 64K / (threads * min CTAs), and a warp
+# scheduler holds 16K registers. 576 and 640 threads trade registers for the
+# 18 or 20 warps per SM that even out the warp tiles of mid-size sheets;
+# lazy staging (values read from shared memory where used) keeps those
+# kernels from spilling.
 _CANDIDATES = [
-    ((256, 1), 2, 0), ((128, 1), 4, 0), ((512, 1), 1, 0), ((192, 1), 3, 0),
-    ((384, 1), 1, 0), ((576, 1), 1, 0), ((640, 1), 1, 0), ((128, 1), 1, 0),
-    ((256, 1), 2, 1), ((128, 1), 4, 1),
+    ((256, 1), 2, 0, False), ((128, 1), 4, 0, False),
+    ((512, 1), 1, 0, False), ((192, 1), 3, 0, False),
+    ((384, 1), 1, 0, False), ((640, 1), 1, 0, False),
+    ((128, 1), 1, 0, False), ((256, 1), 2, 1, False),
+    ((512, 1), 1, 0, True), ((576, 1), 1, 0, True), ((640, 1), 1, 0, True),
+    ((256, 1), 2, 0, True), ((384, 1), 1, 0, True),
 ]
-_CANDIDATES_FP64 = [((128, 1), 1, 0), ((256, 1), 1, 0), ((64, 1), 1, 0),
-                    ((32, 1), 1, 0)]
+_CANDIDATES_FP64 = [((128, 1), 1, 0, False), ((256, 1), 1, 0, False),
+                    ((64, 1), 1, 0, False), ((32, 1), 1, 0, False),
+                    ((256, 1), 1, 0, True)]
 
 
 def _cache_path():
@@ -71,10 +77,11 @@ def lookup(sim):
     return None
 
 
-def _apply(sim, block, min_blocks, spl):
+def _apply(sim, block, min_blocks, spl, lazy=False):
     sim._block = tuple(block)
     sim._min_blocks = int(min_blocks)
     sim._steps_per_launch = int(spl)
+    sim._stage_lazy = bool(lazy)
     sim._graphs = 1
 
 
@@ -97,12 +104,12 @@ def autotune(sim, duration=None, candidates=None, store=True,
             steps = max(4, steps // 20)
         duration = steps * sim.step_size()
     saved = (sim._state.copy(), sim._time, sim._block, sim._min_blocks,
-             sim._steps_per_launch, sim._graphs)
+             sim._steps_per_launch, sim._graphs, sim._stage_lazy)
     results = {}
     try:
         for cand in candidates:
-            block, mb, spl = cand
-            _apply(sim, block, mb, spl)
+            _apply(sim, *cand)
+            block, mb, spl = cand[:3]
             sim._state = saved[0].copy()
             sim._time = saved[1]
             try:
@@ -123,6 +130,7 @@ def autotune(sim, duration=None, candidates=None, store=True,
         sim._state, sim._time = saved[0], saved[1]
         sim._block, sim._min_blocks = saved[2], saved[3]
         sim._steps_per_launch, sim._graphs = saved[4], saved[5]
+        sim._stage_lazy = saved[6]
     if not results:
         return None, results
     best = max(results, key=results.get)
@@ -133,7 +141,9 @@ def autotune(sim, duration=None, candidates=None, store=True,
         d = _load(path)
         d[signature(sim)] = {
             'block': list(best[0]), 'min_blocks': best[1],
-            'steps_per_launch': best[2], 'rate': results[best],
+            'steps_per_launch': best[2],
+            'stage_lazy': bool(best[3]) if len(best) > 3 else False,
+            'rate': results[best],
             'when': time.strftime('%Y-%m-%dT%H:%M:%S')}
         try:
             os.makedirs(os.path.dirname(path), exist_ok=True)

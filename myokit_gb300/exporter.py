@@ -361,12 +361,17 @@ class TissueKernel(object):
     ``row_pad``
         Rows of the grid are not a multiple of 4 cells (2D only): staged
         copies are then 36 cells wide.
+    ``stage_lazy``
+        With staging: read staged values from shared memory where they are
+        used and start the next tile's copies after the computation, instead
+        of reading them all into registers first and copying ahead. Needs
+        fewer registers, so more warps fit on an SM.
     """
     def __init__(self, model, precision, native_math, bound_variables,
                  inter_log, diffusion, two_d, fields, rl_states, block,
                  fast_divide=True, min_blocks=1, math='default',
                  accumulate=None, accumulate_states=(), traj=False,
-                 stage=False, row_pad=False):
+                 stage=False, row_pad=False, stage_lazy=False):
         self.model = model
         self.single = (precision == myokit.SINGLE_PRECISION)
         self.native_math = bool(native_math)
@@ -407,6 +412,7 @@ class TissueKernel(object):
         self.traj = bool(traj)
         self.stage = bool(stage)
         self.row_pad = bool(row_pad) and self.two_d
+        self.stage_lazy = bool(stage_lazy)
         self.layout = None
         if self.stage:
             real = 4 if self.single else 8
@@ -519,11 +525,14 @@ class TissueKernel(object):
         # depend on them are computed per cell here.
         lay = self.layout
         sw = lay['sw'] if lay else 0
+        # Lazy staging binds names to the staged values in shared memory
+        amp = '&' if lay and self.stage_lazy else ''
         field_loads = []
         for k, var in enumerate(self.fields):
             src = (f's_fd[{k * sw}]' if lay else
                    f'field[(long long){k} * pitch + cid]')
-            field_loads.append(f'{tab}const Real {self._name(var)} = {src};')
+            field_loads.append(
+                f'{tab}const Real {amp}{self._name(var)} = {src};')
         body.append(tab + '// Per-cell constants (scalar fields)')
         for eq in const_eqs:
             var = eq.lhs.var()
@@ -565,13 +574,15 @@ class TissueKernel(object):
                 loads.append(f'{tab}const Real {n} = (Real)V_;')
             elif j is not None and self.accumulate == 'double':
                 loads.append(
-                    f'{tab}const double X{n} = {hsrc or hiD + "[" + hplane + "]"};')
+                    f'{tab}const double {amp}X{n} = '
+                    f'{hsrc or hiD + "[" + hplane + "]"};')
                 loads.append(f'{tab}const Real {n} = (Real)X{n};')
             else:
-                loads.append(f'{tab}const Real {n} = {src};')
+                loads.append(f'{tab}const Real {amp}{n} = {src};')
             if j is not None and self.accumulate == 'kahan':
                 loads.append(
-                    f'{tab}const Real C{n} = {hsrc or hiR + "[" + hplane + "]"};')
+                    f'{tab}const Real {amp}C{n} = '
+                    f'{hsrc or hiR + "[" + hplane + "]"};')
             target = 'vout[cid]' if i == self.i_vm else f'state[{plane}]'
             if s in self.rl_states:
                 inf, tau = self.rl_states[s]
@@ -689,6 +700,7 @@ class TissueKernel(object):
         lay = self.layout or {}
         subs.update({
             '@STAGE@': '1' if self.layout else '0',
+            '@STAGE_LAZY@': '1' if self.layout and self.stage_lazy else '0',
             '@SW@': str(lay.get('sw', 32)),
             '@VW@': str(STAGE_VW),
             '@ST_LO@': str(lay.get('lo', 0)),

@@ -251,6 +251,7 @@ class SimulationCUDA(object):
         self._min_blocks = min_blocks
         self._fp32_math = fp32_math
         self._stage_tiles = bool(stage_tiles)
+        self._stage_lazy = None     # set by the autotuner
         if accumulate not in (None, 'double', 'kahan'):
             raise ValueError(
                 'The argument "accumulate" must be None, "double" or'
@@ -757,6 +758,16 @@ class SimulationCUDA(object):
             self._tune_hit = autotune.lookup(self)
         return self._tune_hit
 
+    def _lazy_staging(self):
+        """Staged tiles read where used (True) or prefetched (False)."""
+        if self._stage_lazy is not None:
+            return self._stage_lazy
+        if self._block is None:
+            hit = self._tuned_choice()
+            if hit is not None:
+                return bool(hit.get('stage_lazy', False))
+        return False
+
     def _block_shape(self, two_d):
         """CTA shape (threads, 1); threads is a multiple of the warp size."""
         b = self._block
@@ -838,10 +849,11 @@ class SimulationCUDA(object):
         # are not a multiple of 4 cells need the padded copy width
         stage = self._stage_tiles and self._ntotal >= 256
         row_pad = two_d and self._nx % 4 != 0
+        lazy = stage and self._lazy_staging()
         key = (
             self._model_version, self._precision, self._native_math, mode,
             two_d, block, minb, self._fp32_math, self._accumulate,
-            stage, row_pad, tuple(v.qname() for v in acc),
+            stage, row_pad, lazy, tuple(v.qname() for v in acc),
             tuple(v.qname() for v in self._fields.keys()),
             tuple(v.qname() for v in inter_log))
         k = self._kernels.get(key)
@@ -852,7 +864,7 @@ class SimulationCUDA(object):
                 list(self._fields.keys()), self._rl_states, block,
                 min_blocks=minb, math=self._fp32_math,
                 accumulate=self._accumulate, accumulate_states=acc,
-                stage=stage, row_pad=row_pad)
+                stage=stage, row_pad=row_pad, stage_lazy=lazy)
             if len(self._kernels) > 16:
                 self._kernels.clear()
             self._kernels[key] = k

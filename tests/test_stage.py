@@ -82,8 +82,11 @@ def test_kernels_stage_only_large_grids(br77):
 def _run(model, stage, ncells, precision=SP, rl=False, fields=None,
          gfield=None, conn=None, diffusion=True, dur=4.0, **kw):
     p = myokit.pacing.blocktrain(period=1000, duration=2, offset=0.5)
+    lazy = stage == 'lazy'
     s = mg.SimulationCUDA(model, p, ncells=ncells, precision=precision,
-                          rl=rl, diffusion=diffusion, stage_tiles=stage, **kw)
+                          rl=rl, diffusion=diffusion, stage_tiles=bool(stage),
+                          **kw)
+    s._stage_lazy = lazy
     s.set_step_size(0.01)
     if diffusion and conn is None:
         if isinstance(ncells, tuple):
@@ -113,6 +116,19 @@ def _same(a, b):
         assert np.array_equal(np.asarray(a[1][k]), np.asarray(b[1][k])), k
 
 
+def _close(a, b, tol):
+    # Lazy staging moves the shared-memory reads next to their uses, so the
+    # compiler may contract other multiply-add pairs into FMAs: results
+    # agree to rounding (tol in mV for V; relative for the state)
+    worst = 0.0
+    for k in a[1].keys():
+        x, y = np.asarray(a[1][k]), np.asarray(b[1][k])
+        worst = max(worst, float(np.max(np.abs(x - y))))
+    assert worst <= tol, worst
+    s = np.abs(a[0] - b[0]) / np.maximum(np.abs(a[0]), 1e-6)
+    assert float(np.max(s)) <= 1e3 * tol, float(np.max(s))
+
+
 def _fields(m, shape, names, seed=0):
     rng = np.random.default_rng(seed)
     return {n: m.get(n).eval() * rng.lognormal(0, 0.2, shape) for n in names}
@@ -125,8 +141,9 @@ def test_staged_equals_direct_grid(decker, shape, precision):
     sh = shape[::-1] if isinstance(shape, tuple) else shape
     f = _fields(decker, sh, ['ikr.Gbar', 'ina.Gbar'])
     out = [_run(decker, st, shape, precision, rl=True, fields=f)
-           for st in (False, True)]
+           for st in (False, True, 'lazy')]
     _same(out[0], out[1])
+    _close(out[0], out[2], 1e-3 if precision == SP else 1e-9)
 
 
 @pytest.mark.gpu
@@ -135,8 +152,18 @@ def test_staged_equals_direct_grid(decker, shape, precision):
 def test_staged_equals_direct_accumulate(decker, acc, shape):
     f = _fields(decker, shape[::-1], ['ikr.Gbar'])
     out = [_run(decker, st, shape, SP, rl=True, fields=f, accumulate=acc)
-           for st in (False, True)]
+           for st in (False, True, 'lazy')]
     _same(out[0], out[1])
+    _close(out[0], out[2], 1e-3)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('block', [512, 640])
+def test_lazy_staging_with_wide_ctas(decker, block):
+    f = _fields(decker, (40, 70), ['ikr.Gbar'])
+    out = [_run(decker, st, (70, 40), SP, rl=True, fields=f, block=block,
+                min_blocks=1) for st in (False, 'lazy')]
+    _close(out[0], out[1], 1e-3)
 
 
 @pytest.mark.gpu
@@ -149,8 +176,10 @@ def test_staged_equals_direct_hetero(br77, shape):
     else:
         g = (rng.uniform(5, 10, shape - 1),)
         g[0][::97] = 0     # separate cables
-    out = [_run(br77, st, shape, DP, gfield=g) for st in (False, True)]
+    out = [_run(br77, st, shape, DP, gfield=g)
+           for st in (False, True, 'lazy')]
     _same(out[0], out[1])
+    _close(out[0], out[2], 1e-9)
 
 
 @pytest.mark.gpu
