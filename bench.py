@@ -76,6 +76,9 @@ def parse():
     p.add_argument('--profile', action='store_true',
                    help='run one small sheet case for a profiler and exit')
     p.add_argument('--profile-steps', type=int, default=40)
+    p.add_argument('--no-fields', action='store_true',
+                   help='with --profile: a sheet without scalar fields (the'
+                        ' 2048x2048 S1-S2 configuration)')
     p.add_argument('--profile-adjoint', action='store_true',
                    help='with --profile: run the discrete adjoint (loss on'
                         ' 64 probes, checkpoints every 200 steps) instead')
@@ -83,8 +86,9 @@ def parse():
                    help='resident CTAs per SM asked for the reverse kernel')
     p.add_argument('--adj-threads', type=int, default=0,
                    help='CTA size of the reverse kernel (0: the forward\'s)')
-    p.add_argument('--adj-no-guards', action='store_true',
-                   help='straight-line reverse sweep')
+    p.add_argument('--adj-guards', action='store_true',
+                   help='reverse sweep with a zero-adjoint branch per'
+                        ' equation (default: straight-line)')
     p.add_argument('--no-stage', action='store_true',
                    help='profile the kernel that reads tiles from global'
                         ' memory instead of staging them with TMA')
@@ -105,7 +109,7 @@ def load_model():
     return myokit.load_model(path)
 
 
-def make_sheet(cls, precision, size, seed=0, **kw):
+def make_sheet(cls, precision, size, seed=0, fields=True, **kw):
     """The benchmark sheet; returns (simulation, log variable list)."""
     from myokit_gb300._deps import myokit
     m = load_model()
@@ -116,8 +120,9 @@ def make_sheet(cls, precision, size, seed=0, **kw):
     rng = np.random.default_rng(seed)
     gkr = m.get('ikr.Gbar').eval()
     gna = m.get('ina.Gbar').eval()
-    s.set_field('ikr.Gbar', gkr * rng.lognormal(0, 0.2, (size, size)))
-    s.set_field('ina.Gbar', gna * rng.lognormal(0, 0.2, (size, size)))
+    if fields:
+        s.set_field('ikr.Gbar', gkr * rng.lognormal(0, 0.2, (size, size)))
+        s.set_field('ina.Gbar', gna * rng.lognormal(0, 0.2, (size, size)))
     cells = rng.choice(size * size, 256, replace=False)
     log = ['engine.time'] + [
         '%d.%d.membrane.V' % (c % size, c // size) for c in sorted(cells)]
@@ -605,7 +610,7 @@ def profile_case(args):
         adj = ad.TissueAdjoint(s, probes, segment_steps=200,
                                min_blocks=args.adj_min_blocks,
                                threads=args.adj_threads or None,
-                               guards=not args.adj_no_guards)
+                               guards=args.adj_guards)
         ms = args.profile_steps * 0.005
         out = {}
         for _ in range(2):
@@ -622,19 +627,24 @@ def profile_case(args):
         print(json.dumps(dict(out, size=args.size, steps=args.profile_steps,
                               adj_min_blocks=args.adj_min_blocks,
                               adj_threads=args.adj_threads,
-                              guards=not args.adj_no_guards,
+                              guards=args.adj_guards,
                               staged=s._last_kernel.layout is not None)))
         return 0
     s, log = make_sheet(mg.SimulationCUDA, prec, args.size,
+                        fields=not args.no_fields,
                         steps_per_launch=args.profile_steps, accumulate=acc,
                         stage_tiles=not args.no_stage)
     ms = args.profile_steps * 0.005
     for _ in range(2):
         s.run(ms, log=log, log_interval=1)
     st = s.last_run_stats()
+    k = s._last_kernel
     print(json.dumps({'size': args.size, 'precision': args.precision,
                       'accumulate': args.accumulate,
-                      'staged': s._last_kernel.layout is not None,
+                      'staged': k.layout is not None,
+                      'lazy': bool(k.layout) and k.stage_lazy,
+                      'block': k.block[0], 'min_blocks': k.min_blocks,
+                      'bytes_per_cell_step': k.bytes_per_cell_step(),
                       'steps': st['cell_steps']
                       // (args.size * args.size), 'launches': st['launches'],
                       'kernel_ms': st['kernel_ms']}))

@@ -504,6 +504,8 @@ void fill_launch(mkg_sim *s, mkg_launch *a)
     a->nbr_g = s->d_nbr_g;
     a->gxs = s->gx;
     a->gys = s->gy;
+    a->gxf = (float)s->gx;
+    a->gyf = (float)s->gy;
     a->pace_x0 = s->px0;
     a->pace_x1 = s->px1;
     a->pace_y0 = s->py0;
@@ -1210,7 +1212,9 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
         h.t = rec.t;
         h.dt = rec.dt;
         h.pace = rec.pace;
-        h.pad = 0;
+        h.tf = (float)rec.t;
+        h.dtf = (float)rec.dt;
+        h.pacef = (float)rec.pace;
         if (rec.log) {
             h.log_row = (int)rows;
             if (s->real == 4) {

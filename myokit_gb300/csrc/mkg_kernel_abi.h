@@ -24,8 +24,9 @@ typedef struct mkg_step {
     double t;          /* engine time at the start of the step */
     double dt;         /* step size */
     double pace;       /* global pacing level during the step */
+    float tf, dtf, pacef;  /* the same, rounded to single precision on the
+                              host (what a single precision kernel uses) */
     int log_row;       /* row of the chunk log written at this step, or -1 */
-    int pad;
 } mkg_step;
 
 /* Device-side status word, one per simulation. */
@@ -50,6 +51,7 @@ typedef struct mkg_launch {
     const int *nbr_idx;      /* CSR neighbour cell ids */
     const void *nbr_g;       /* CSR conductances (Real) */
     double gxs, gys;         /* homogeneous conductances */
+    float gxf, gyf;          /* the same, rounded to single precision */
     long long pace_x0, pace_x1, pace_y0, pace_y1;  /* paced rectangle */
     const unsigned int *pace_bits;                 /* paced list bitmap */
     const mkg_step *steps;   /* nsteps schedule entries */

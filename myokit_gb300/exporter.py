@@ -257,6 +257,20 @@ def _pow_helpers(single):
     return '\n'.join(out)
 
 
+def _constant_subtrees(e):
+    """The largest subexpressions of ``e`` that reference no variable and
+    are more than a number (conditions are kept, their operands searched)."""
+    if isinstance(e, myokit.Number):
+        return []
+    if not isinstance(e, myokit.Condition) and not any(
+            True for _ in e.references()):
+        return [e]
+    out = []
+    for op in e:
+        out.extend(_constant_subtrees(op))
+    return out
+
+
 def _read(name):
     with open(os.path.join(_CSRC, name), 'r') as f:
         return f.read()
@@ -507,8 +521,13 @@ class TissueKernel(object):
 
         def fold(e):
             if literal_subst:
-                return e.clone(subst=literal_subst)
-            return e
+                e = e.clone(subst=literal_subst)
+            # Subexpressions of literals only (e.g. sqrt(Ko / 5.4) beside a
+            # per-cell field) are evaluated here, like the folded constants
+            sub = {}
+            for c in _constant_subtrees(e):
+                sub[c] = myokit.Number(float(c.eval(precision=prec)))
+            return e.clone(subst=sub) if sub else e
 
         body = []
         tab = '        '
