@@ -75,6 +75,10 @@ def parse():
                         ' 2048x2048 sheet instead of a 20 ms window')
     p.add_argument('--profile', action='store_true',
                    help='run one small sheet case for a profiler and exit')
+    p.add_argument('--tune', action='store_true',
+                   help='autotune the launch shape of every benchmark'
+                        ' configuration, print the timings and the table'
+                        ' (the format of myokit_gb300/tuned.json), exit')
     p.add_argument('--profile-steps', type=int, default=40)
     p.add_argument('--no-fields', action='store_true',
                    help='with --profile: a sheet without scalar fields (the'
@@ -482,28 +486,13 @@ def config_c3(args, device):
     Decker 2009 model stands in for ten Tusscher 2006. Timed over 20 ms.
     """
     from myokit_gb300._deps import myokit
-    import myokit_gb300 as mg
-    rng = np.random.default_rng(3)
-    lengths = rng.integers(50, 2001, 512)
-    n = int(lengths.sum())
-    starts = np.concatenate([[0], np.cumsum(lengths)[:-1]])
     m = load_model()
     p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
-    names = ['ina.Gbar', 'inal.Gbar', 'ik1.Gbar', 'ikr.Gbar', 'ito.Gbar',
-             'ikur.Gbar']
-    out = {'cables': 512, 'cells': n}
+    out = {}
     for spl in (100, 0):
-        s = mg.SimulationCUDA(m, p, ncells=n, rl=True, accumulate='kahan',
-                              steps_per_launch=spl, device=device)
-        s.set_step_size(0.01)
-        g = np.full(n - 1, 10.0)
-        g[starts[1:] - 1] = 0
-        s.set_conductance_field(g)
-        for name in names:
-            base = m.get(name).eval()
-            s.set_field(name, np.repeat(
-                base * rng.lognormal(0, 0.3, 512), lengths))
-        s.set_paced_cell_list([int(a + k) for a in starts for k in range(5)])
+        s, batch = _cables(m, p, steps_per_launch=spl, device=device)
+        out['cables'] = len(batch.lengths)
+        out['cells'] = batch.ncells
         s.run(2, log=['engine.time'], log_interval=1)
         s.run(20, log=['engine.time'], log_interval=1)
         st = s.last_run_stats()
@@ -511,6 +500,25 @@ def config_c3(args, device):
             'value': st['cell_steps'] / (st['kernel_ms'] / 1000),
             'unit': UNIT, 'launches': st['launches'], 'window_ms': 20}
     return out
+
+
+CABLE_FIELDS = ['ina.Gbar', 'inal.Gbar', 'ik1.Gbar', 'ikr.Gbar', 'ito.Gbar',
+                'ikur.Gbar']
+
+
+def _cables(m, p, **kw):
+    """The 512 batched cables: lengths uniform 50-2000 (seed 3), six
+    conductances x lognormal(0, 0.3) per cable, first 5 cells paced,
+    g = 10 inside a cable, dt 0.01 ms, FP32 + Kahan."""
+    from myokit_gb300.batch import CableBatch
+    rng = np.random.default_rng(3)
+    lengths = rng.integers(50, 2001, 512)
+    fields = {name: m.get(name).eval() * rng.lognormal(0, 0.3, 512)
+              for name in CABLE_FIELDS}
+    batch = CableBatch(m, lengths, p, conductance=10.0, paced_cells=5,
+                       fields=fields, rl=True, accumulate='kahan', **kw)
+    batch.sim.set_step_size(0.01)
+    return batch.sim, batch
 
 
 def config_c5(args, device):
@@ -587,6 +595,57 @@ def config_c5(args, device):
     out['fp64'] = {'value': v64, 'unit': UNIT, 'window_ms': 1}
     out['speedup_over_fp64'] = out['value'] / v64
     return out
+
+
+def tune_configs(args):
+    """
+    Runs the autotuner on each benchmark configuration: the 512 x 512 sheet
+    in every precision mode, the 2048 x 2048 sheet (FP32 and Kahan), the
+    512 batched cables and the 200-cell cable. Results go to the user cache
+    (MYOKIT_GB300_CACHE or ~/.cache/myokit_gb300); the table is printed.
+    """
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+    from myokit_gb300 import autotune as at
+    SP, DP = myokit.SINGLE_PRECISION, myokit.DOUBLE_PRECISION
+
+    def tune(name, s):
+        t0 = time.time()
+        best, res = at.autotune(s)
+        print(json.dumps({'config': name, 'best': str(best), 'seconds':
+                          round(time.time() - t0, 1), 'rates': {
+                              str(k): round(v / 1e9, 3)
+                              for k, v in res.items()}}), flush=True)
+
+    for label, prec, kw in [('fp32', SP, {}),
+                            ('kahan', SP, {'accumulate': 'kahan'}),
+                            ('double', SP, {'accumulate': 'double'}),
+                            ('ieee', SP, {'fp32_math': 'ieee'}),
+                            ('fp64', DP, {})]:
+        s, _ = make_sheet(mg.SimulationCUDA, prec, 512, **kw)
+        tune('sheet512-' + label, s)
+    m = load_model()
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    for label, kw in (('kahan', {'accumulate': 'kahan'}), ('fp32', {})):
+        s = mg.SimulationCUDA(m, p, ncells=(2048, 2048), rl=True, **kw)
+        s.set_step_size(0.005)
+        s.set_paced_cells(nx=4, ny=2048, x=0, y=0)
+        tune('sheet2048-' + label, s)
+    s, _ = _cables(m, p)
+    tune('cables512-kahan', s)
+    br = myokit.load_model(os.path.join(
+        os.path.dirname(myokit.__file__), 'tests', 'data',
+        'beeler-1977-model.mmt'))
+    for label, prec, kw in (('fp64', DP, {}),
+                            ('kahan', SP, {'accumulate': 'kahan'})):
+        s = mg.SimulationCUDA(br, p, ncells=200, precision=prec, **kw)
+        s.set_step_size(0.005)
+        s.set_conductance(9)
+        s.set_paced_cells(5)
+        tune('cable200-' + label, s)
+    with open(at._cache_path()) as f:
+        print(f.read())
+    return 0
 
 
 def profile_case(args):
@@ -898,6 +957,8 @@ def main():
         return run_reference(args)
     if args.profile:
         return profile_case(args)
+    if args.tune:
+        return tune_configs(args)
     return run_ours(args)
 
 
