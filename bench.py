@@ -324,9 +324,10 @@ def accuracy_runs(args, device):
 def adjoint_runs(args, device):
     """
     The discrete adjoint on a 256 x 256 sheet of the bench configuration
-    (single precision): loss = sum of squared V errors at 64 probes every
-    1 ms against a target made with seed-perturbed GKr/GNa fields; gradient
-    with respect to both fields and gx, gy; checkpoints every 200 steps.
+    (single precision forward with V and concentrations in FP64): loss =
+    sum of squared V errors at 64 probes every 1 ms against a target made
+    with seed-perturbed GKr/GNa fields; gradient with respect to both
+    fields and gx, gy; checkpoints every 200 steps.
     Reports adjoint time / forward time, and a central finite-difference
     check (relative step 1e-4, double precision, 64 x 64 sheet, 20 random
     entries).
@@ -343,11 +344,11 @@ def adjoint_runs(args, device):
     probes = [(int(c % n), int(c // n)) for c in cells]
     keys = ['%d.%d.membrane.V' % p for p in probes]
     s, _ = make_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION, n,
-                      seed=1, device=device)
+                      seed=1, device=device, accumulate='double')
     adj = ad.TissueAdjoint(s, probes, segment_steps=200)
     target = adj.forward(dur, 1.0)
     s, _ = make_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION, n,
-                      seed=0, device=device)
+                      seed=0, device=device, accumulate='double')
     adj = ad.TissueAdjoint(s, probes, segment_steps=200)
     adj.loss_and_gradient(min(dur, 5.0), target[:int(min(dur, 5.0))], 1.0)
     s.run(min(dur, 5.0), log=['engine.time'] + keys, log_interval=1)
@@ -365,6 +366,8 @@ def adjoint_runs(args, device):
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     out['sheet256_fp32'] = {
+        'precision': 'fp32 with FP64 V and concentrations',
+        'accumulated_states': [x.qname() for x in s.accumulated_states()],
         'window_ms': dur, 'probes': len(probes), 'segment_steps': 200,
         'forward_s': t_fwd, 'adjoint_forward_s': t1 - t0,
         'adjoint_backward_s': t2 - t1,

@@ -193,9 +193,6 @@ class AdjointKernel(object):
         if fwd.diffusion not in (_exp.DIFF_NONE, _exp.DIFF_GRID):
             raise NotImplementedError(
                 'The adjoint supports homogeneous grid diffusion only.')
-        if fwd.accumulate is not None:
-            raise NotImplementedError(
-                'The adjoint runs without accumulation modes.')
         self.fwd = fwd
         self.single = fwd.single
         self.min_blocks = int(min_blocks)
@@ -374,9 +371,13 @@ class TissueAdjoint(object):
     Forward runs and loss gradients for a :class:`SimulationCUDA`.
 
     ``sim``
-        A simulation with homogeneous grid diffusion (1D or 2D) or none, and
-        no accumulation mode. Its fields are the parameters the gradients
-        refer to; its conductance gives gx, gy.
+        A simulation with homogeneous grid diffusion (1D or 2D) or none.
+        Its fields are the parameters the gradients refer to; its
+        conductance gives gx, gy. With an accumulation mode the forward
+        runs (and is recomputed) exactly as the simulation's own, FP64 or
+        compensated states included; the reverse sweep is in the
+        simulation precision and takes the rounding of those states to it
+        as the identity.
     ``probes``
         Cells whose V enters the loss: integers (1D) or ``(x, y)`` (2D).
     ``segment_steps``
@@ -398,9 +399,6 @@ class TissueAdjoint(object):
     """
     def __init__(self, sim, probes, segment_steps=200, min_blocks=1,
                  threads=None, guards=False):
-        if sim._accumulate is not None:
-            raise NotImplementedError(
-                'The adjoint runs without accumulation modes.')
         self.sim = sim
         self.segment_steps = int(segment_steps)
         self.min_blocks = int(min_blocks)
@@ -448,7 +446,10 @@ class TissueAdjoint(object):
                 sim._bound_variables, [], kernel.diffusion, kernel.two_d,
                 list(sim._fields.keys()), sim._rl_states, kernel.block,
                 min_blocks=kernel.min_blocks, math=sim._fp32_math,
-                traj=True, stage=kernel.stage, row_pad=kernel.row_pad)
+                accumulate=kernel.accumulate,
+                accumulate_states=sim.accumulated_states(), traj=True,
+                stage=kernel.stage, row_pad=kernel.row_pad,
+                stage_lazy=kernel.stage_lazy)
             ak = AdjointKernel(fwd, self.min_blocks, self.threads,
                                self.guards)
             self._generated = {akey: ak}

@@ -292,6 +292,7 @@ struct mkg_sim {
     cudaKernel_t adj_fwd = nullptr, adj_bwd = nullptr;
     int adj_occ_fwd = 1, adj_occ_bwd = 1;
     int adj_bwd_threads = 0;              /* reverse kernel CTA size */
+    size_t ckpt_bytes = 0;                /* bytes per checkpoint */
     int adj_seg = 0;                      /* steps per checkpoint segment */
     void *d_traj = nullptr, *d_lam = nullptr, *d_mu = nullptr;
     void *d_gfield = nullptr, *d_gg = nullptr, *d_lgrad = nullptr;
@@ -1615,9 +1616,6 @@ extern "C" int mkg_adj_attach(mkg_sim *s, const void *cubin, size_t size,
 {
     if (!s || !cubin || !size) return set_err(s, MKG_ERR_ARG, "null argument");
     if (seg_steps < 1) return set_err(s, MKG_ERR_ARG, "seg_steps < 1");
-    if (s->cfg.hi_mode != MKG_HI_NONE)
-        return set_err(s, MKG_ERR_ARG,
-                       "the adjoint runs without accumulation modes");
     if (s->cfg.diffusion != MKG_DIFF_NONE &&
         s->cfg.diffusion != MKG_DIFF_GRID)
         return set_err(s, MKG_ERR_ARG,
@@ -1685,11 +1683,19 @@ extern "C" int mkg_adj_forward(mkg_sim *s, double tmin, double tmax,
     s->adj_log.clear();
     s->adj_rows = 0;
     const size_t plane = (size_t)s->pitch * s->real;
-    const size_t ckpt_bytes = plane * (s->cfg.n_state + 1);
+    const size_t vplane = (size_t)s->pitch * s->vbytes;
+    const size_t hi_bytes = s->d_hi ? (size_t)s->pitch * 8 * s->cfg.n_hi : 0;
+    const size_t ckpt_bytes = plane * s->cfg.n_state + vplane + hi_bytes;
+    if (s->ckpt_bytes != ckpt_bytes) {
+        for (void *p : s->adj_ckpt) cudaFree(p);
+        s->adj_ckpt.clear();
+        s->ckpt_bytes = ckpt_bytes;
+    }
     size_t nseg = 0;
     int status = MKG_OK;
     while (status == MKG_OK) {
-        /* Checkpoint: state planes and the current V plane */
+        /* Checkpoint: state planes, the current V plane and the
+         * accumulation planes (FP64 states or compensation terms) */
         if (nseg >= s->adj_ckpt.size()) {
             void *p = nullptr;
             CK(s, cudaMalloc(&p, ckpt_bytes));
@@ -1699,8 +1705,12 @@ extern "C" int mkg_adj_forward(mkg_sim *s, double tmin, double tmax,
         CK(s, cudaMemcpyAsync(ck, s->d_state, plane * s->cfg.n_state,
                               cudaMemcpyDeviceToDevice, s->stream));
         CK(s, cudaMemcpyAsync(ck + plane * s->cfg.n_state,
-                              (char *)s->d_vbuf + (size_t)s->v_sel * plane,
-                              plane, cudaMemcpyDeviceToDevice, s->stream));
+                              (char *)s->d_vbuf + (size_t)s->v_sel * vplane,
+                              vplane, cudaMemcpyDeviceToDevice, s->stream));
+        if (hi_bytes)
+            CK(s, cudaMemcpyAsync(ck + plane * s->cfg.n_state + vplane,
+                                  s->d_hi, hi_bytes,
+                                  cudaMemcpyDeviceToDevice, s->stream));
         s->adj_seg_vsel.push_back(s->v_sel);
         double t = 0;
         int64_t rows = 0;
@@ -1853,11 +1863,17 @@ int adj_backward(mkg_sim *s, const double *lgrad, int64_t rows,
         /* Restore the segment's checkpoint */
         const char *ck = (const char *)s->adj_ckpt[g];
         const int vsel = s->adj_seg_vsel[g];
+        const size_t vplane = (size_t)s->pitch * s->vbytes;
         CK(s, cudaMemcpyAsync(s->d_state, ck, plane * s->cfg.n_state,
                               cudaMemcpyDeviceToDevice, s->stream));
-        CK(s, cudaMemcpyAsync((char *)s->d_vbuf + (size_t)vsel * plane,
-                              ck + plane * s->cfg.n_state, plane,
+        CK(s, cudaMemcpyAsync((char *)s->d_vbuf + (size_t)vsel * vplane,
+                              ck + plane * s->cfg.n_state, vplane,
                               cudaMemcpyDeviceToDevice, s->stream));
+        if (s->d_hi && s->cfg.n_hi > 0)
+            CK(s, cudaMemcpyAsync(s->d_hi,
+                                  ck + plane * s->cfg.n_state + vplane,
+                                  (size_t)s->pitch * 8 * s->cfg.n_hi,
+                                  cudaMemcpyDeviceToDevice, s->stream));
         /* Forward over the segment, recording the trajectory */
         mkg_launch a;
         fill_launch(s, &a);

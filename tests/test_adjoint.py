@@ -55,9 +55,10 @@ def test_local_partials_match_numerical(name):
     assert checked > 20
 
 
-def _sim(model, precision, shape=(6, 5), rl=False, fields=None):
+def _sim(model, precision, shape=(6, 5), rl=False, fields=None, cls=None):
     p = myokit.pacing.blocktrain(period=1000, duration=2, offset=1)
-    s = mg.SimulationCUDA(model, p, ncells=shape, precision=precision, rl=rl)
+    cls = cls or mg.SimulationCUDA
+    s = cls(model, p, ncells=shape, precision=precision, rl=rl)
     s.set_paced_cells(2, shape[1] if isinstance(shape, tuple) else 1)
     s.set_conductance(9, 6)
     for name, values in (fields or {}).items():
@@ -204,3 +205,75 @@ def test_guarded_and_straight_line_sweeps_agree(br77):
         np.testing.assert_allclose(np.asarray(out[0][1][k]),
                                    np.asarray(out[1][1][k]), rtol=1e-12,
                                    atol=0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('acc', ['double', 'kahan'])
+def test_adjoint_with_accumulation_modes(br77, acc):
+    # FP32 forward with FP64 (or compensated) V and concentrations: the
+    # adjoint's forward equals the simulation's own run, and its gradients
+    # agree with the double precision adjoint to the FP32 forward's accuracy
+    shape = (5, 6)
+    f0 = _fields(br77, shape, 1)
+    p = myokit.pacing.blocktrain(period=1000, duration=2, offset=1)
+    res = {}
+    for key, kw in (('fp64', {'precision': DP}),
+                    (acc, {'precision': SP, 'accumulate': acc})):
+        s = mg.SimulationCUDA(br77, p, ncells=(6, 5), **kw)
+        s.set_paced_cells(2, 5)
+        s.set_conductance(9, 6)
+        for k, v in f0.items():
+            s.set_field(k, v)
+        adj = adjoint.TissueAdjoint(s, PROBES, segment_steps=70)
+        target = np.zeros((24, len(PROBES))) - 80
+        L, g = adj.loss_and_gradient(12, target, 0.5)
+        res[key] = (L, g)
+        if key == acc:
+            keys = ['engine.time'] + ['%d.%d.membrane.V' % q for q in PROBES]
+            va = adj.forward(12, 0.5)
+            d = s.run(12, log=keys, log_interval=0.5)
+            v = np.stack([np.asarray(d[k]) for k in keys[1:]], axis=1)
+            assert np.array_equal(v, va)
+    L64, g64 = res['fp64']
+    L32, g32 = res[acc]
+    assert abs(L32 - L64) <= 1e-3 * L64
+    for k in g64:
+        a, b = np.asarray(g32[k]), np.asarray(g64[k])
+        err = np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30)
+        assert err <= 2e-2, (k, err)
+
+
+@pytest.mark.gpu
+def test_adjoint_matches_oracle_finite_differences(br77):
+    # Gradients of the loss as the reference computes it: central finite
+    # differences of the oracle's (reference SimulationOpenCL) loss
+    from oracle.refsim import ReferenceCpuSimulation
+    shape = (5, 6)
+    f0 = _fields(br77, shape, 1)
+    target = np.zeros((24, len(PROBES))) - 80
+    s = _sim(br77, DP, fields=f0)
+    adj = adjoint.TissueAdjoint(s, PROBES, segment_steps=100)
+    L, grads = adj.loss_and_gradient(12, target, 0.5)
+    keys = ['%d.%d.membrane.V' % q for q in PROBES]
+
+    def oracle_loss(fields, gx=9.0):
+        o = _sim(br77, DP, fields=fields, cls=ReferenceCpuSimulation)
+        o.set_conductance(gx, 6)
+        d = o.run(12, log=['engine.time'] + keys, log_interval=0.5)
+        v = np.stack([np.asarray(d[k]) for k in keys], axis=1)
+        return float(np.sum((v - target) ** 2))
+
+    assert abs(oracle_loss(f0) - L) <= 1e-9 * L
+    for name, idx in (('isi.gsBar', (0, 0)), ('isi.gsBar', (2, 3)),
+                      ('ina.gNaBar', (4, 5)), ('ina.gNaBar', (1, 1))):
+        h = 1e-4 * f0[name][idx]
+        vals = []
+        for sgn in (1, -1):
+            f = {k: v.copy() for k, v in f0.items()}
+            f[name][idx] += sgn * h
+            vals.append(oracle_loss(f))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert abs(grads[name][idx] - fd) <= 1e-4 * max(abs(fd), 1e-6 * L)
+    h = 1e-4 * 9.0
+    fd = (oracle_loss(f0, 9.0 + h) - oracle_loss(f0, 9.0 - h)) / (2 * h)
+    assert abs(grads['gx'] - fd) <= 1e-4 * abs(fd)
