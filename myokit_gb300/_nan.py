@@ -131,7 +131,7 @@ def find_nan(sim, log, watch_var=None, safe_range=None, return_log=False):
         istart = ifirst - 1
         state = _cell_state(sim, log, istart)
         t0 = log[time_var][istart]
-        saved = (sim._state, sim._time)
+        saved = (sim._state.copy(), sim._time)
         sim._state = np.array(state, dtype=float)
         sim._time = t0
         try:
@@ -193,7 +193,7 @@ def find_nan(sim, log, watch_var=None, safe_range=None, return_log=False):
     if return_log:
         istart = max(0, ifirst - max_states)
         state = _cell_state(sim, log, istart)
-        saved = (sim._state, sim._time)
+        saved = (sim._state.copy(), sim._time)
         sim._state = np.array(state, dtype=float)
         sim._time = times[-1]
         try:

@@ -229,6 +229,8 @@ class SimulationCUDA(object):
         if self._diffusion_enabled:
             self.set_paced_cells()
         self._fields = OrderedDict()
+        self._field_block = None    # fields interleaved per cell, pinned
+        self._pinned = {}           # page-locked host buffers by use
         self.set_step_size()
         self._time = 0
         self._nstate = self._model.count_states()
@@ -603,6 +605,7 @@ class SimulationCUDA(object):
                     'The argument `values` must have dimensions ' + str(shape)
                     + '.')
         self._fields[var] = values.reshape(self._nx * self._ny).copy()
+        self._field_block = None
 
     def remove_field(self, var):
         """Removes the field set for ``var``."""
@@ -610,6 +613,7 @@ class SimulationCUDA(object):
             var = var.qname()
         var = self._model.get(var)
         del self._fields[var]
+        self._field_block = None
 
     # ------------------------------------------------------------------
     # State and time
@@ -1047,15 +1051,36 @@ class SimulationCUDA(object):
             self._report_nan(log)
         return log
 
+    def _host_buffer(self, use, n):
+        """
+        A page-locked float64 host array of ``n`` values, one per ``use``
+        ('state', 'fields'), reused between runs: copies from and to it are
+        DMA transfers without a pageable staging copy. ``self._state`` is
+        the 'state' buffer after a run, so code that keeps the state across
+        a run keeps a copy.
+        """
+        buf = self._pinned.get(use)
+        if buf is None or buf[1].size != n:
+            import torch
+            t = torch.empty(n, dtype=torch.float64, pin_memory=True)
+            buf = (t, t.numpy())
+            self._pinned[use] = buf
+        return buf[1]
+
     def _upload(self, be):
         """Copies state, fields, conductances, pacing and protocol."""
         lib, h = be.lib, be.h
         st = np.ascontiguousarray(self._state, dtype=np.float64)
         be.check(lib.mkg_set_state(h, _lib.dptr(st), st.size))
         if self._fields:
-            fd = np.ascontiguousarray(
-                np.stack([np.asarray(v, dtype=float)
-                          for v in self._fields.values()], axis=1))
+            if self._field_block is None:
+                fd = self._host_buffer('fields',
+                                       len(self._fields) * self._ntotal)
+                fd.reshape(self._ntotal, -1)[:] = np.stack(
+                    [np.asarray(v, dtype=float)
+                     for v in self._fields.values()], axis=1)
+                self._field_block = fd
+            fd = self._field_block
             be.check(lib.mkg_set_fields(h, _lib.dptr(fd), fd.size))
         mode = self._diffusion_mode()
         if mode == _exp.DIFF_GRID:
@@ -1179,7 +1204,7 @@ class SimulationCUDA(object):
 
         # Final state (openclsim.c:1185-1190); on an exception above the
         # state is left unchanged, as in the reference.
-        st = np.empty(self._nstate * self._ntotal)
+        st = self._host_buffer('state', self._nstate * self._ntotal)
         be.check(lib.mkg_get_state(h, _lib.dptr(st), st.size))
         self._state = st
 
@@ -1273,7 +1298,7 @@ class SimulationCUDA(object):
                     cs += ncs.value
             finally:
                 lib.mkg_set_frame_buffer(h, None, 0)
-            st = np.empty(self._nstate * self._ntotal)
+            st = self._host_buffer('state', self._nstate * self._ntotal)
             be.check(lib.mkg_get_state(h, _lib.dptr(st), st.size))
             self._state = st
             self._last_stats = {'kernel_ms': ms, 'cell_steps': cs,
