@@ -100,6 +100,20 @@ typedef struct mkg_config {
 int mkg_stage_layout(const mkg_config *cfg, int64_t *out);
 
 /*
+ * Couples a fiber simulation (sim, whose kernel is a fused fiber-tissue
+ * kernel) to a tissue simulation (partner): from then on mkg_run_chunk on
+ * sim advances both in one launch per chunk, with the junction current
+ * gft (Vf - Vt) between fiber cell (nx - 1, y) and tissue cell (0, cty + y)
+ * for every fiber row y. The partner's log rows of a chunk are read with
+ * mkg_read_log(partner, ...). Replaces the two diff_step launches, the
+ * diff_step_fiber_tissue launch and the two cell_step launches of each step
+ * of the reference's fiber-tissue loop (fiber_tissue.c:1003-1130,
+ * openclsim.cl:601-628). A NULL partner uncouples.
+ */
+int mkg_set_partner(mkg_sim *sim, mkg_sim *partner, double gft,
+                    int64_t cty);
+
+/*
  * Compiles generated CUDA C++ source to an sm_103a cubin with NVRTC.
  * Replaces clCreateProgramWithSource + clBuildProgram (openclsim.c:812-839).
  * On success *cubin (size *cubin_size) and *log are malloc'd; free them with

@@ -279,6 +279,11 @@ struct mkg_sim {
     bool use_graphs = false;  /* replay multi-launch chunks as CUDA graphs */
     std::map<std::string, cudaGraphExec_t> graphs;
 
+    /* Fiber-tissue: a second simulation (the tissue) advanced by this
+     * one's fused kernel, and the junction between them (not owned) */
+    mkg_sim *partner = nullptr;
+    mkg_junction junction;
+
     /* Device frame buffer for log rows (not owned) */
     void *frame_buf = nullptr;
     int64_t frame_rows = 0, frame_next = 0;
@@ -1157,6 +1162,10 @@ int mkg_run_begin(mkg_sim *s, double tmin, double tmax, double default_dt,
         int r = mkg_set_log(s, nullptr, nullptr, 0, 0);
         if (r) return r;
     }
+    if (s->partner && !s->partner->d_log_cols) {
+        int r = mkg_set_log(s->partner, nullptr, nullptr, 0, 0);
+        if (r) return set_err(s, r, "%s", mkg_last_error(s->partner));
+    }
     clear_graphs(s);
     const int st = s->sched.begin(s->pacer, tmin, tmax, default_dt,
                                   log_interval);
@@ -1196,8 +1205,17 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
             return set_err(s, MKG_ERR_ARG, "the frame buffer is full");
         row_cap = std::max<int64_t>(row_cap, 0);
     }
+    mkg_sim *p = s->partner;
+    if (p) {
+        const int64_t pcol = std::max(p->log_ncol, 1);
+        row_cap = std::min<int64_t>(
+            row_cap, std::max<int64_t>(16, (int64_t)(256ll << 20) /
+                                               (pcol * 8)));
+    }
     int r = ensure_schedule(s, max_steps, row_cap);
     if (r) return r;
+    if (p && (r = ensure_schedule(p, 1, row_cap)))
+        return set_err(s, r, "%s", mkg_last_error(p));
 
     /* Host schedule for this chunk (openclsim.c:1051-1162). */
     int64_t n = 0, rows = 0;
@@ -1248,7 +1266,19 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
         a.stage_tx = (int)s->lay.tx;
     }
     const int threads = bx * by;
-    const long long nblocks = blocks_needed(s, &a);
+    /* The partner's launch block: its buffers, log and pacing; steps,
+     * status and barrier are this simulation's */
+    mkg_launch b;
+    if (p) {
+        fill_launch(p, &b);
+        b.status = s->d_status;
+        b.steps = nullptr;
+    }
+    const long long nblocks =
+        p ? ((long long)(a.ntiles_x * (long long)a.ntiles_y +
+                         b.ntiles_x * (long long)b.ntiles_y) * 32 +
+             threads - 1) / threads
+          : blocks_needed(s, &a);
     int bpsm = s->blocks_per_sm > 0 ? std::min(s->blocks_per_sm, s->occ_blocks)
                                     : s->occ_blocks;
     long long coop_blocks = std::min<long long>(nblocks,
@@ -1270,7 +1300,9 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
     CK(s, cudaEventRecord(s->ev0, s->stream));
 
     const int64_t nlaunch = (n + spl - 1) / spl;
-    const bool graph = s->use_graphs && nlaunch > 1;
+    /* (graphs are not used with a partner, whose log buffers may grow
+     * between chunks) */
+    const bool graph = s->use_graphs && nlaunch > 1 && !p;
     const int v_sel0 = s->v_sel;
     cudaGraphExec_t exec = nullptr;
     if (graph) {
@@ -1294,6 +1326,7 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
             a.epoch_base = epoch;
             a.v_sel = diffusion_on(s) ? (v_sel0 ^ (int)(off & 1)) : 0;
             void *args[] = {&a, &s->tmaps};
+            void *args_p[] = {&a, &b, &s->junction};
             cudaLaunchConfig_t lc;
             memset(&lc, 0, sizeof(lc));
             cudaLaunchAttribute attr[1];
@@ -1313,7 +1346,7 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
             lc.gridDim = dim3((unsigned)grid, 1, 1);
             lc.dynamicSmemBytes = s->tile_smem;
             const cudaError_t e = cudaLaunchKernelExC(
-                &lc, (const void *)s->kernel, args);
+                &lc, (const void *)s->kernel, p ? args_p : args);
             if (e != cudaSuccess) {
                 if (graph) {
                     cudaGraph_t g = nullptr;
@@ -1358,6 +1391,7 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
         halted = true;
     }
     if (diffusion_on(s)) s->v_sel = v_sel0 ^ (int)(done & 1);
+    if (p) p->v_sel = s->v_sel;
     s->last_cell_steps = done * s->ncell;
 
     /* Rows written by the executed steps */
@@ -1380,6 +1414,21 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
         CK(s, cudaMemcpyAsync(s->h_log, s->d_log_dbl, cnt * sizeof(double),
                               cudaMemcpyDeviceToHost, s->stream));
     }
+    if (p && rows_done > 0 && p->log_ncol > 0) {
+        /* The partner's rows, through the same stream */
+        const long long cnt = rows_done * (long long)p->log_ncol;
+        s->n_launches++;
+        if (p->real == 4)
+            k_log_to_double<float><<<grid_for(cnt), 256, 0, s->stream>>>(
+                (const float *)p->d_log, p->d_log_dbl, cnt);
+        else
+            k_log_to_double<double><<<grid_for(cnt), 256, 0, s->stream>>>(
+                (const double *)p->d_log, p->d_log_dbl, cnt);
+        CK(s, cudaGetLastError());
+        CK(s, cudaMemcpyAsync(p->h_log, p->d_log_dbl, cnt * sizeof(double),
+                              cudaMemcpyDeviceToHost, s->stream));
+    }
+    if (p) p->last_rows = rows_done;
     CK(s, cudaStreamSynchronize(s->stream));
     float ms = 0;
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
@@ -1421,6 +1470,38 @@ int mkg_last_stats(const mkg_sim *s, double *kernel_ms, int64_t *launches,
     if (kernel_ms) *kernel_ms = s->last_ms;
     if (launches) *launches = s->last_launches;
     if (cell_steps) *cell_steps = s->last_cell_steps;
+    return MKG_OK;
+}
+
+int mkg_set_partner(mkg_sim *s, mkg_sim *partner, double gft, int64_t cty)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (!partner) {
+        s->partner = nullptr;
+        clear_graphs(s);
+        return MKG_OK;
+    }
+    const mkg_config &c = s->cfg, &d = partner->cfg;
+    if (partner == s || c.device != d.device || c.real_bytes != d.real_bytes)
+        return set_err(s, MKG_ERR_ARG,
+                       "the partner must be another simulation of the same"
+                       " precision on the same device");
+    if (c.diffusion != MKG_DIFF_GRID || d.diffusion != MKG_DIFF_GRID ||
+        !c.two_d || !d.two_d || c.stage || d.stage ||
+        c.hi_mode != MKG_HI_NONE || d.hi_mode != MKG_HI_NONE)
+        return set_err(s, MKG_ERR_ARG,
+                       "fiber-tissue simulations use 2D grid diffusion"
+                       " without staging or accumulation modes");
+    if (c.ny > d.ny || cty < 0 || cty + c.ny > d.ny)
+        return set_err(s, MKG_ERR_ARG,
+                       "the junction rows must lie inside the tissue");
+    clear_graphs(s);
+    s->partner = partner;
+    s->junction.gft = gft;
+    s->junction.gftf = (float)gft;
+    s->junction.nfy = (int)c.ny;
+    s->junction.cty = cty;
+    partner->v_sel = s->v_sel;
     return MKG_OK;
 }
 

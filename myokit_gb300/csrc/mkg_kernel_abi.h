@@ -98,6 +98,15 @@ typedef struct mkg_tmaps {
     mkg_tmap gx;             /* Real[nx - 1]: 1D heterogeneous conductances */
 } mkg_tmaps;
 
+/* The fiber-tissue junction: fiber cell (nfx - 1, y) and tissue cell
+ * (0, cty + y), y < nfy, are coupled by the conductance gft. */
+typedef struct mkg_junction {
+    double gft;
+    float gftf;              /* gft rounded to single precision */
+    int nfy;
+    long long cty;
+} mkg_junction;
+
 /* Arguments of the adjoint kernel: one checkpoint segment in reverse. */
 typedef struct mkg_adj_launch {
     mkg_launch f;            /* geometry, fields, pacing, schedule, status */

@@ -716,6 +716,11 @@ class TissueKernel(object):
             '@BODY@': '\n'.join(body),
             '@LOG_B@': log_b,
         }
+        # The per-cell pieces, for kernels that assemble several models
+        self.parts = {
+            'loads': subs['@LOADS@'], 'log_a': log_a,
+            'body': subs['@BODY@'], 'log_b': log_b,
+        }
         lay = self.layout or {}
         subs.update({
             '@STAGE@': '1' if self.layout else '0',
@@ -795,3 +800,57 @@ class TissueKernel(object):
         """Arithmetic operations per cell-step (excluding transcendentals),
         plus about 8 for the diffusion current."""
         return self.census.arith + (8 if self.diffusion else 0)
+
+
+class FiberTissueKernel(object):
+    """
+    One fused kernel for ``FiberTissueSimulationCUDA``: the fiber's and the
+    tissue's generated cell code (from two :class:`TissueKernel` objects,
+    both for homogeneous 2D grid diffusion without staging) in one launch,
+    with the junction current between the fiber's last column and the
+    tissue's first (``openclsim.cl:601-628``).
+    """
+    def __init__(self, fiber, tissue):
+        if fiber.single != tissue.single:
+            raise ValueError('Both kernels must have the same precision.')
+        if fiber.block != tissue.block:
+            raise ValueError('Both kernels must have the same CTA shape.')
+        for k in (fiber, tissue):
+            if k.diffusion != DIFF_GRID or not k.two_d or k.layout:
+                raise ValueError('Fiber-tissue kernels use 2D homogeneous'
+                                 ' diffusion without tile staging.')
+        self.fiber = fiber
+        self.tissue = tissue
+        self.single = fiber.single
+        self.block = fiber.block
+        self.min_blocks = fiber.min_blocks
+        text = _read('fiber_tissue_kernel.cu.in')
+        subs = {
+            '@REAL@': 'float' if self.single else 'double',
+            '@SINGLE@': '1' if self.single else '0',
+            '@BX@': str(self.block[0]),
+            '@MINB@': str(self.min_blocks),
+            '@POW_HELPERS@': _pow_helpers(self.single),
+        }
+        for name, k in (('FIBER', fiber), ('TISSUE', tissue)):
+            for part in ('loads', 'log_a', 'body', 'log_b'):
+                subs['@%s_%s@' % (name, part.upper())] = k.parts[part]
+        for key, v in subs.items():
+            text = text.replace(key, v)
+        self._source = (
+            '// Generated by myokit_gb300.exporter for models '
+            + str(fiber.model.name()) + ' (fiber) and '
+            + str(tissue.model.name()) + ' (tissue)\n'
+            + _read('mkg_kernel_abi.h') + '\n' + text)
+
+    def source(self):
+        return self._source
+
+    def options(self):
+        return self.fiber.options()
+
+    def key(self):
+        h = hashlib.sha256()
+        h.update(self._source.encode())
+        h.update('\0'.join(self.options()).encode())
+        return h.hexdigest()
