@@ -449,7 +449,7 @@ class TissueAdjoint(object):
                 accumulate=kernel.accumulate,
                 accumulate_states=sim.accumulated_states(), traj=True,
                 stage=kernel.stage, row_pad=kernel.row_pad,
-                stage_lazy=kernel.stage_lazy)
+                stage_lazy=kernel.stage_lazy, sync=kernel.sync)
             ak = AdjointKernel(fwd, self.min_blocks, self.threads,
                                self.guards)
             self._generated = {akey: ak}

@@ -19,22 +19,28 @@ import numpy as np
 from ._deps import myokit
 
 # Candidate (threads per CTA, min CTAs per SM, steps per launch, lazy tile
-# staging); the register cap is 64K / (threads * min CTAs), and a warp
-# scheduler holds 16K registers. 576 and 640 threads trade registers for the
-# 18 or 20 warps per SM that even out the warp tiles of mid-size sheets;
-# lazy staging (values read from shared memory where used) keeps those
-# kernels from spilling.
+# staging, step synchronisation). The register cap is 64K / (threads * min
+# CTAs), and a warp scheduler holds 16K registers. 576 and 640 threads trade
+# registers for the 18 or 20 warps per SM that even out the warp tiles of
+# mid-size sheets; lazy staging (values read from shared memory where used)
+# keeps those kernels from spilling. Steps are separated by a grid barrier
+# or by waits on the neighbouring warps only.
+_B, _N = 'barrier', 'neighbors'
 _CANDIDATES = [
-    ((256, 1), 2, 0, False), ((128, 1), 4, 0, False),
-    ((512, 1), 1, 0, False), ((192, 1), 3, 0, False),
-    ((384, 1), 1, 0, False), ((640, 1), 1, 0, False),
-    ((128, 1), 1, 0, False), ((256, 1), 2, 1, False),
-    ((512, 1), 1, 0, True), ((576, 1), 1, 0, True), ((640, 1), 1, 0, True),
-    ((256, 1), 2, 0, True), ((384, 1), 1, 0, True),
+    ((256, 1), 2, 0, False, _B), ((128, 1), 4, 0, False, _B),
+    ((512, 1), 1, 0, False, _B), ((192, 1), 3, 0, False, _B),
+    ((384, 1), 1, 0, False, _B), ((640, 1), 1, 0, False, _B),
+    ((128, 1), 1, 0, False, _B), ((256, 1), 2, 1, False, _B),
+    ((512, 1), 1, 0, True, _B), ((576, 1), 1, 0, True, _B),
+    ((640, 1), 1, 0, True, _B), ((256, 1), 2, 0, True, _B),
+    ((384, 1), 1, 0, True, _B),
+    ((512, 1), 1, 0, False, _N), ((384, 1), 1, 0, False, _N),
+    ((256, 1), 2, 0, False, _N), ((640, 1), 1, 0, True, _N),
+    ((256, 1), 2, 0, True, _N),
 ]
-_CANDIDATES_FP64 = [((128, 1), 1, 0, False), ((256, 1), 1, 0, False),
-                    ((64, 1), 1, 0, False), ((32, 1), 1, 0, False),
-                    ((256, 1), 1, 0, True)]
+_CANDIDATES_FP64 = [((128, 1), 1, 0, False, _B), ((256, 1), 1, 0, False, _B),
+                    ((64, 1), 1, 0, False, _B), ((32, 1), 1, 0, False, _B),
+                    ((256, 1), 1, 0, True, _B), ((256, 1), 1, 0, False, _N)]
 
 
 def _cache_path():
@@ -77,11 +83,12 @@ def lookup(sim):
     return None
 
 
-def _apply(sim, block, min_blocks, spl, lazy=False):
+def _apply(sim, block, min_blocks, spl, lazy=False, sync='barrier'):
     sim._block = tuple(block)
     sim._min_blocks = int(min_blocks)
     sim._steps_per_launch = int(spl)
     sim._stage_lazy = bool(lazy)
+    sim._sync = sync
     sim._graphs = 1
 
 
@@ -104,7 +111,7 @@ def autotune(sim, duration=None, candidates=None, store=True,
             steps = max(4, steps // 20)
         duration = steps * sim.step_size()
     saved = (sim._state.copy(), sim._time, sim._block, sim._min_blocks,
-             sim._steps_per_launch, sim._graphs, sim._stage_lazy)
+             sim._steps_per_launch, sim._graphs, sim._stage_lazy, sim._sync)
     results = {}
     try:
         for cand in candidates:
@@ -130,7 +137,7 @@ def autotune(sim, duration=None, candidates=None, store=True,
         sim._state, sim._time = saved[0], saved[1]
         sim._block, sim._min_blocks = saved[2], saved[3]
         sim._steps_per_launch, sim._graphs = saved[4], saved[5]
-        sim._stage_lazy = saved[6]
+        sim._stage_lazy, sim._sync = saved[6], saved[7]
     if not results:
         return None, results
     best = max(results, key=results.get)
@@ -143,6 +150,7 @@ def autotune(sim, duration=None, candidates=None, store=True,
             'block': list(best[0]), 'min_blocks': best[1],
             'steps_per_launch': best[2],
             'stage_lazy': bool(best[3]) if len(best) > 3 else False,
+            'sync': best[4] if len(best) > 4 else 'barrier',
             'rate': results[best],
             'when': time.strftime('%Y-%m-%dT%H:%M:%S')}
         try:

@@ -235,6 +235,8 @@ struct mkg_sim {
     double *d_log_dbl = nullptr;
     mkg_step *d_steps = nullptr;
     mkg_status *d_status = nullptr;
+    unsigned int *d_warp_epoch = nullptr;  /* per-warp step counters */
+    size_t n_warp_epoch = 0;
     double *d_stage = nullptr;   /* staging for double uploads */
     void *d_hi = nullptr;        /* accumulation planes [n_hi][pitch] x 8 B */
     int *d_hi_slot = nullptr;    /* per state: accumulation plane or -1 */
@@ -527,6 +529,7 @@ void fill_launch(mkg_sim *s, mkg_launch *a)
     a->status = s->d_status;
     a->timeout_ns = s->timeout_ns;
     a->hi = s->d_hi;
+    a->warp_epoch = s->d_warp_epoch;
     /* Warp tiles: 32 consecutive cells of a row (2D) or of the flat cell
      * array (1D cables, connection graphs, diffusion-free simulations). */
     if (s->cfg.two_d) {
@@ -730,6 +733,7 @@ void mkg_destroy(mkg_sim *s)
     dfree(s->d_log_dbl);
     dfree(s->d_steps);
     dfree(s->d_status);
+    dfree(s->d_warp_epoch);
     dfree(s->d_stage);
     dfree(s->d_hi);
     dfree(s->d_hi_slot);
@@ -853,6 +857,11 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
     }
     CKC(cudaMalloc((void **)&s->d_status, sizeof(mkg_status)));
     CKC(cudaMallocHost((void **)&s->h_status, sizeof(mkg_status)));
+    /* One step counter per warp of the largest co-resident grid */
+    s->n_warp_epoch = (size_t)s->occ_blocks * s->num_sms *
+                      (size_t)(cfg->block_x / 32);
+    CKC(cudaMalloc((void **)&s->d_warp_epoch,
+                   s->n_warp_epoch * sizeof(unsigned int)));
     CKC(cudaStreamSynchronize(s->stream));
 #undef CKC
     *out = s;
@@ -1297,6 +1306,8 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
     *s->h_status = init;
     CK(s, cudaMemcpyAsync(s->d_status, s->h_status, sizeof(mkg_status),
                           cudaMemcpyHostToDevice, s->stream));
+    CK(s, cudaMemsetAsync(s->d_warp_epoch, 0,
+                          s->n_warp_epoch * sizeof(unsigned int), s->stream));
     CK(s, cudaEventRecord(s->ev0, s->stream));
 
     const int64_t nlaunch = (n + spl - 1) / spl;
@@ -1728,6 +1739,17 @@ extern "C" int mkg_adj_attach(mkg_sim *s, const void *cubin, size_t size,
         &s->adj_occ_bwd, (const void *)s->adj_bwd, s->adj_bwd_threads, 0));
     if (s->adj_occ_fwd < 1 || s->adj_occ_bwd < 1)
         return set_err(s, MKG_ERR_CUDA, "adjoint kernels cannot be resident");
+    {
+        /* The trajectory kernel's grid may be larger than the forward's */
+        const size_t nw = (size_t)s->adj_occ_fwd * s->num_sms *
+                          (size_t)(s->cfg.block_x / 32);
+        if (nw > s->n_warp_epoch) {
+            dfree(s->d_warp_epoch);
+            CK(s, cudaMalloc((void **)&s->d_warp_epoch,
+                             nw * sizeof(unsigned int)));
+            s->n_warp_epoch = nw;
+        }
+    }
     const size_t plane = (size_t)s->pitch * s->real;
     dfree(s->d_traj);
     dfree(s->d_lam);
@@ -1967,6 +1989,9 @@ int adj_backward(mkg_sim *s, const double *lgrad, int64_t rows,
         a.traj = s->d_traj;
         if (s->cfg.stage) a.stage_tx = (int)s->lay.tx;
         CK(s, cudaMemsetAsync(&s->d_status->barrier, 0, sizeof(unsigned),
+                              s->stream));
+        CK(s, cudaMemsetAsync(s->d_warp_epoch, 0,
+                              s->n_warp_epoch * sizeof(unsigned int),
                               s->stream));
         int r = launch_coop(s, s->adj_fwd, &a, s->adj_occ_fwd,
                             blocks_needed(s, &a), s->tile_smem);

@@ -81,6 +81,8 @@ typedef struct mkg_launch {
                                 compensation terms */
     void *traj;              /* adjoint forward pass only: the states at t
                                 of every step, Real[nsteps][n_state][pitch] */
+    unsigned int *warp_epoch; /* neighbour synchronisation: steps completed
+                                by each warp of the grid (reset per chunk) */
 } mkg_launch;
 
 /* An opaque TMA tensor map (CUtensorMap: 128 bytes, 64-byte aligned) */

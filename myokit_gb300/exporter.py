@@ -375,6 +375,10 @@ class TissueKernel(object):
     ``row_pad``
         Rows of the grid are not a multiple of 4 cells (2D only): staged
         copies are then 36 cells wide.
+    ``sync``
+        ``'barrier'``: a grid-wide barrier between steps; ``'neighbors'``:
+        each warp waits only for the warps owning its halo tiles (per-warp
+        step counters). Connection graphs always use the barrier.
     ``stage_lazy``
         With staging: read staged values from shared memory where they are
         used and start the next tile's copies after the computation, instead
@@ -385,7 +389,8 @@ class TissueKernel(object):
                  inter_log, diffusion, two_d, fields, rl_states, block,
                  fast_divide=True, min_blocks=1, math='default',
                  accumulate=None, accumulate_states=(), traj=False,
-                 stage=False, row_pad=False, stage_lazy=False):
+                 stage=False, row_pad=False, stage_lazy=False,
+                 sync='barrier'):
         self.model = model
         self.single = (precision == myokit.SINGLE_PRECISION)
         self.native_math = bool(native_math)
@@ -427,6 +432,10 @@ class TissueKernel(object):
         self.stage = bool(stage)
         self.row_pad = bool(row_pad) and self.two_d
         self.stage_lazy = bool(stage_lazy)
+        if sync not in ('barrier', 'neighbors'):
+            raise ValueError('sync must be "barrier" or "neighbors"')
+        # Connection graphs have arbitrary neighbours: grid barrier only
+        self.sync = sync if self.diffusion != DIFF_CONN else 'barrier'
         self.layout = None
         if self.stage:
             real = 4 if self.single else 8
@@ -723,6 +732,7 @@ class TissueKernel(object):
         }
         lay = self.layout or {}
         subs.update({
+            '@NBR_SYNC@': '1' if self.sync == 'neighbors' else '0',
             '@STAGE@': '1' if self.layout else '0',
             '@STAGE_LAZY@': '1' if self.layout and self.stage_lazy else '0',
             '@SW@': str(lay.get('sw', 32)),

@@ -254,6 +254,9 @@ class SimulationCUDA(object):
         self._fp32_math = fp32_math
         self._stage_tiles = bool(stage_tiles)
         self._stage_lazy = None     # set by the autotuner
+        # Between steps: 'barrier' (grid-wide) or 'neighbors' (each warp
+        # waits for the warps whose cells it reads); None: tuned or barrier
+        self._sync = None
         if accumulate not in (None, 'double', 'kahan'):
             raise ValueError(
                 'The argument "accumulate" must be None, "double" or'
@@ -762,6 +765,16 @@ class SimulationCUDA(object):
             self._tune_hit = autotune.lookup(self)
         return self._tune_hit
 
+    def _sync_mode(self):
+        """How steps are separated: 'barrier' or 'neighbors'."""
+        if self._sync is not None:
+            return self._sync
+        if self._block is None:
+            hit = self._tuned_choice()
+            if hit is not None:
+                return hit.get('sync', 'barrier')
+        return 'barrier'
+
     def _lazy_staging(self):
         """Staged tiles read where used (True) or prefetched (False)."""
         if self._stage_lazy is not None:
@@ -857,7 +870,8 @@ class SimulationCUDA(object):
         key = (
             self._model_version, self._precision, self._native_math, mode,
             two_d, block, minb, self._fp32_math, self._accumulate,
-            stage, row_pad, lazy, tuple(v.qname() for v in acc),
+            stage, row_pad, lazy, self._sync_mode(),
+            tuple(v.qname() for v in acc),
             tuple(v.qname() for v in self._fields.keys()),
             tuple(v.qname() for v in inter_log))
         k = self._kernels.get(key)
@@ -868,7 +882,8 @@ class SimulationCUDA(object):
                 list(self._fields.keys()), self._rl_states, block,
                 min_blocks=minb, math=self._fp32_math,
                 accumulate=self._accumulate, accumulate_states=acc,
-                stage=stage, row_pad=row_pad, stage_lazy=lazy)
+                stage=stage, row_pad=row_pad, stage_lazy=lazy,
+                sync=self._sync_mode())
             if len(self._kernels) > 16:
                 self._kernels.clear()
             self._kernels[key] = k

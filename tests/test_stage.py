@@ -213,3 +213,28 @@ def test_staged_matches_oracle_fp64(br77, shape):
         worst = max(worst, float(np.max(np.abs(
             np.asarray(res[0][k]) - np.asarray(res[1][k])))))
     assert worst < FP64_TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('stage', [False, True, 'lazy'])
+@pytest.mark.parametrize('shape', [(64, 20), (37, 23), 1000])
+def test_neighbour_sync_equals_grid_barrier(decker, stage, shape):
+    # Waiting only for the warps that own a warp's halo tiles gives the
+    # same results as a grid-wide barrier between steps
+    out = []
+    for sync in ('barrier', 'neighbors'):
+        p = myokit.pacing.blocktrain(period=1000, duration=2, offset=0.5)
+        s = mg.SimulationCUDA(decker, p, ncells=shape, rl=True,
+                              stage_tiles=bool(stage), block=64,
+                              min_blocks=1)
+        s._stage_lazy = stage == 'lazy'
+        s._sync = sync
+        if isinstance(shape, tuple):
+            s.set_paced_cells(3, shape[1])
+        else:
+            s.set_paced_cells(5)
+        s.set_step_size(0.01)
+        d = s.run(4, log=['engine.time', 'membrane.V'], log_interval=0.5)
+        assert s._last_kernel.sync == sync
+        out.append((s.state_array(), d))
+    _same(out[0], out[1])
