@@ -725,7 +725,9 @@ def run_reference(args):
                         args.size)
     s.set_threads(cores)
     ncell = args.size * args.size
-    # Bench step: a bounded sample sized to ~2 s of CPU time
+    # Bench step: a bounded sample sized to ~2 s of CPU time (calibrated
+    # after a first run, which also builds the reference kernel)
+    s.run(0.05, log=log, log_interval=1)
     t0 = time.perf_counter()
     s.run(0.05, log=log, log_interval=1)
     rate0 = ncell * 10 / max(time.perf_counter() - t0, 1e-9)
