@@ -217,7 +217,8 @@ def test_staged_matches_oracle_fp64(br77, shape):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize('stage', [False, True, 'lazy'])
-@pytest.mark.parametrize('shape', [(64, 20), (37, 23), 1000])
+@pytest.mark.parametrize('shape', [(64, 20), (37, 23), 1000, (2000, 1),
+                                   (3, 400), 300])
 def test_neighbour_sync_equals_grid_barrier(decker, stage, shape):
     # Waiting only for the warps that own a warp's halo tiles gives the
     # same results as a grid-wide barrier between steps
@@ -238,3 +239,26 @@ def test_neighbour_sync_equals_grid_barrier(decker, stage, shape):
         assert s._last_kernel.sync == sync
         out.append((s.state_array(), d))
     _same(out[0], out[1])
+
+
+@pytest.mark.gpu
+def test_neighbour_sync_nan_halt():
+    # A NaN halt stops every warp after the halting step, with neighbour
+    # synchronisation as with the grid barrier
+    import test_oracle as to
+    msgs = []
+    for sync in ('barrier', 'neighbors'):
+        p = myokit.Protocol()
+        p.schedule(start=0, level=-80, duration=1.234)
+        p.schedule(start=1.234, level=-47.13, duration=1000)
+        s = mg.SimulationCUDA(to._nan_model(), p, ncells=(64, 40), block=64,
+                              min_blocks=1)
+        s.set_paced_cell_list([[1, 1]])
+        s._sync = sync
+        s._steps_per_launch = 7
+        with pytest.raises(myokit.SimulationError) as e:
+            s.run(5)
+        assert s._last_kernel.sync == sync
+        msgs.append(str(e.value))
+    assert 'Time:  1.23' in msgs[0]
+    assert msgs[0] == msgs[1]
