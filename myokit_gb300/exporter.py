@@ -8,22 +8,25 @@ diffusion kernels (``diff_step`` ``:384``, ``diff_hetero`` ``:452``,
 ``diff_arb_step`` ``:537``). This exporter emits a single CUDA kernel,
 ``mkg_tissue_step``, that for every cell and step
 
-1. computes the diffusion current from V(t) of the neighbours (shared-memory
-   halo tile for 2D grids, neighbour list for arbitrary connections),
+1. computes the diffusion current from V(t) of the neighbours (warp tiles
+   staged in shared memory by TMA tensor copies, or loaded directly;
+   neighbour lists for arbitrary connections),
 2. evaluates the model right-hand side in registers,
 3. writes the logged values of that step to the device log, and
 4. updates every state to t + dt, writing V(t + dt) to the second plane of a
    ping-pong buffer so that neighbours still read V(t).
 
-Several steps run in one launch, separated by a bounded grid barrier. State
-is stored structure-of-arrays, so every load and store is coalesced.
+Several steps run in one launch, separated by a bounded grid barrier or by
+bounded waits on the warps owning the neighbouring tiles. State is stored
+structure-of-arrays, so every load and store is coalesced.
 
 Differences from the reference kernel text that do not change results:
 
 - constants that do not depend on a scalar field are evaluated once on the
   host (in the simulation precision, with ``Expression.eval``) and written as
   literals, where the reference writes them as macros (``openclsim.cl:174-186``);
-- small integer powers ``x^2``, ``x^3``, ``x^4`` are written as products.
+- subexpressions of literals only are evaluated on the host as well;
+- small integer powers ``x^2`` .. ``x^16`` are written as products.
 """
 import hashlib
 import os
