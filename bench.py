@@ -813,11 +813,10 @@ def run_ours(args):
         cell_steps += st['cell_steps']
     barrier()
     clocks = sampler.stop()
-    if dist is not None:
-        t = torch.tensor([dev_ms, wall], dtype=torch.float64, device='cuda')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms, wall = float(t[0]), float(t[1])
-    total_cell_steps = cell_steps * world
+    # Replicas: the slowest rank's times, every rank's cell-steps
+    from myokit_gb300.replicas import combine
+    dev_ms, wall, total_cell_steps = combine(
+        dev_ms, wall, cell_steps, world, dist, 'cuda')
     value = total_cell_steps / (dev_ms / 1000.0)
     e2e_value = total_cell_steps / wall
 
