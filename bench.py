@@ -73,6 +73,10 @@ def parse():
     p.add_argument('--c5-full', action='store_true',
                    help='run the whole 1000 ms S1-S2 protocol of the'
                         ' 2048x2048 sheet instead of a 20 ms window')
+    p.add_argument('--full', action='store_true',
+                   help='run every configuration at its full length: the'
+                        ' batched cables for 2000 ms, the adjoint over'
+                        ' 300 ms, the 2048x2048 S1-S2 protocol for 1000 ms')
     p.add_argument('--profile', action='store_true',
                    help='run one small sheet case for a profiler and exit')
     p.add_argument('--tune', action='store_true',
@@ -338,7 +342,7 @@ def adjoint_runs(args, device):
     from myokit_gb300 import adjoint as ad
     out = {}
     n = 256
-    dur = args.adjoint_ms
+    dur = 300.0 if args.full else args.adjoint_ms
     rng = np.random.default_rng(5)
     cells = rng.choice(n * n, 64, replace=False)
     probes = [(int(c % n), int(c // n)) for c in cells]
@@ -496,12 +500,22 @@ def config_c3(args, device):
         s, batch = _cables(m, p, steps_per_launch=spl, device=device)
         out['cables'] = len(batch.lengths)
         out['cells'] = batch.ncells
+        window = 2000 if (args.full and spl == 100) else 20
         s.run(2, log=['engine.time'], log_interval=1)
-        s.run(20, log=['engine.time'], log_interval=1)
+        t0 = time.perf_counter()
+        d = s.run(window, log=['engine.time'] + batch.cable_log_keys(
+            len(batch.lengths) - 1)[-1:], log_interval=1)
+        wall = time.perf_counter() - t0
         st = s.last_run_stats()
         out['steps_per_launch_%d' % spl] = {
             'value': st['cell_steps'] / (st['kernel_ms'] / 1000),
-            'unit': UNIT, 'launches': st['launches'], 'window_ms': 20}
+            'e2e': st['cell_steps'] / wall,
+            'unit': UNIT, 'launches': st['launches'], 'window_ms': window}
+        if window == 2000:
+            # The last cable's far end fires once per paced beat
+            v = np.asarray(d[batch.cable_log_keys(
+                len(batch.lengths) - 1)[-1]])
+            out['last_cable_end_max_v_mV'] = float(v.max())
     return out
 
 
@@ -546,7 +560,7 @@ def config_c5(args, device):
     s.reset()
     out = {'grid': [n, n]}
     torch.cuda.synchronize()
-    if args.c5_full:
+    if args.c5_full or args.full:
         t0 = time.perf_counter()
         t1_, f1 = s.run_frames(320, 5)
         ms = s.last_run_stats()['kernel_ms']
