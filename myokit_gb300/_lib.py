@@ -58,6 +58,8 @@ class MkgConfig(ctypes.Structure):
 
 # Every symbol declared in include/mkg_tissue.h, with its signature
 SIGNATURES = {
+    'mkg_set_wait': (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32]),
     'mkg_set_partner': (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int64]),
     'mkg_stage_layout': (ctypes.c_int, [

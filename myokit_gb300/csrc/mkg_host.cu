@@ -269,6 +269,7 @@ struct mkg_sim {
     int steps_per_launch = 0;
     int blocks_per_sm = 0;
     long long timeout_ns = 2000000000LL;
+    int wait_skew = 0;        /* mkg_set_wait: unreachable step waits */
 
     mkg::Pacer pacer;
     mkg::Schedule sched;
@@ -528,6 +529,7 @@ void fill_launch(mkg_sim *s, mkg_launch *a)
     a->nan_check = s->nan_check;
     a->status = s->d_status;
     a->timeout_ns = s->timeout_ns;
+    a->wait_skew = s->wait_skew;
     a->hi = s->d_hi;
     a->warp_epoch = s->d_warp_epoch;
     /* Warp tiles: 32 consecutive cells of a row (2D) or of the flat cell
@@ -1481,6 +1483,18 @@ int mkg_last_stats(const mkg_sim *s, double *kernel_ms, int64_t *launches,
     if (kernel_ms) *kernel_ms = s->last_ms;
     if (launches) *launches = s->last_launches;
     if (cell_steps) *cell_steps = s->last_cell_steps;
+    return MKG_OK;
+}
+
+int mkg_set_wait(mkg_sim *s, int64_t timeout_ns, int32_t skew)
+{
+    if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
+    if (timeout_ns < 1000000 || timeout_ns > 60000000000LL || skew < 0)
+        return set_err(s, MKG_ERR_ARG,
+                       "the wait bound must be 1 ms to 60 s, the skew >= 0");
+    clear_graphs(s);
+    s->timeout_ns = timeout_ns;
+    s->wait_skew = skew;
     return MKG_OK;
 }
 

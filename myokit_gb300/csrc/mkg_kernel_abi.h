@@ -75,7 +75,9 @@ typedef struct mkg_launch {
     int epoch_base;          /* grid barriers completed by earlier launches
                                 of this chunk (the barrier counter is reset
                                 once per chunk) */
-    int pad1;
+    int wait_skew;           /* added to every step-wait target: 0, or > 0
+                                to make the waits unreachable (a test of
+                                the bounded-wait path) */
     void *hi;                /* accumulation planes [n_hi][pitch], 8 bytes
                                 per entry: FP64 states, or FP32 Kahan
                                 compensation terms */
