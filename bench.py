@@ -851,6 +851,18 @@ def run_ours(args):
         traffic_per_launch = traffic['bytes_per_cell_step'] * per_launch_cs
     # Compute roofline: FP32 lanes x 2 flops x SM clock under load
     sm_mhz = clocks['sm_mhz'] if clocks else 1900.0
+    # Instruction-issue roofline (what binds the L2-resident sheet): warp
+    # instructions per cell-step from the committed ncu capture, against
+    # 4 warp schedulers x 152 SMs issuing one instruction per clock
+    issue = None
+    if traffic and traffic.get('warp_instructions_per_cell_step'):
+        ach = traffic['warp_instructions_per_cell_step'] * value / world
+        peak_i = 4 * 152 * sm_mhz * 1e6
+        issue = {'unit': 'warp instructions/s', 'achieved': ach,
+                 'peak': peak_i, 'frac': ach / peak_i,
+                 'warp_instructions_per_cell_step':
+                     traffic['warp_instructions_per_cell_step'],
+                 'source': traffic.get('source')}
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     flops = kernel.flops_per_cell_step() * value / world / 1e12
 
@@ -954,6 +966,7 @@ def run_ours(args):
                 'flops_per_cell_step': kernel.flops_per_cell_step(),
                 'transcendentals_per_cell_step': kernel.census.trans,
                 'peak_source': 'FP32 lanes x 2 x median SM clock'},
+            'issue': issue,
         },
         'fp64': fp64,
         'variants': variants,
