@@ -657,6 +657,18 @@ class TissueKernel(object):
                     body.append(text)
                     emitted.add(i)
 
+        # The derivative of a Rush-Larsen state is not needed for its update.
+        # The reference skips its equation but still declares it, as a
+        # component output initialised to zero (openclsim.cl:236-238,
+        # 341-343), so other equations that refer to dot(x) see 0. The same
+        # zero is defined here for the derivatives that are referred to.
+        used_dots = set()
+        for group in order.values():
+            for eq in group.equations(const=False):
+                for r in eq.rhs.references():
+                    if isinstance(r, myokit.Derivative):
+                        used_dots.add(r.var())
+
         # Equations in solvable order (the reference calls one function per
         # component in this order, openclsim.cl:336-352).
         body.append(tab + '// Model right-hand side at time t')
@@ -668,8 +680,11 @@ class TissueKernel(object):
                     continue
                 if isinstance(eq.lhs, myokit.Derivative) and \
                         var in self.rl_states:
-                    continue
-                rhs = fold(eq.rhs)
+                    if var not in used_dots:
+                        continue
+                    rhs = myokit.Number(0)
+                else:
+                    rhs = fold(eq.rhs)
                 self.rhs_eqs.append((eq.lhs, rhs))
                 self.census.add(rhs)
                 name = self._name(eq.lhs)

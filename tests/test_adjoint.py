@@ -277,3 +277,56 @@ def test_adjoint_matches_oracle_finite_differences(br77):
     h = 1e-4 * 9.0
     fd = (oracle_loss(f0, 9.0 + h) - oracle_loss(f0, 9.0 - h)) / (2 * h)
     assert abs(grads['gx'] - fd) <= 1e-4 * abs(fd)
+
+
+def _dep_model():
+    # Other equations refer to dot(m) of a Rush-Larsen state (ina.x) and to
+    # dot(V) (test.t1); the file has no membrane_potential label
+    m = load('lr-1991-dep.mmt')
+    m.get('membrane.V').set_label('membrane_potential')
+    return m
+
+
+def test_adjoint_kernel_with_derivative_references_compiles():
+    m = _dep_model()
+    s = _sim(m, DP, rl=True, fields={'ina.gNa': np.full((5, 6), 16.0)})
+    k = s._kernel([])
+    # m and h update by Rush-Larsen; other equations see dot(m) = dot(h) = 0,
+    # as in the reference's kernel
+    assert 'const Real d_m = 0' in k.source()
+    assert 'const Real d_h = 0' in k.source()
+    fwd = exporter.TissueKernel(
+        s._model, s._precision, False, s._bound_variables, [], k.diffusion,
+        k.two_d, list(s._fields.keys()), s._rl_states, k.block, traj=True)
+    ak = adjoint.AdjointKernel(fwd, guards=False)
+    cubin, _ = _lib.compile_source(ak.source(), ak.options())
+    assert cubin[:4] == b'\x7fELF'
+
+
+@pytest.mark.gpu
+def test_adjoint_with_derivative_references():
+    m = _dep_model()
+    shape = (5, 6)
+    rng = np.random.default_rng(4)
+    f0 = 16.0 * rng.lognormal(0, 0.2, shape)
+    ft = 16.0 * rng.lognormal(0, 0.2, shape)
+    s = _sim(m, DP, rl=True, fields={'ina.gNa': ft})
+    adj = adjoint.TissueAdjoint(s, PROBES, segment_steps=150)
+    target = adj.forward(12, 0.5)
+    s.set_field('ina.gNa', f0)
+    L, grads = adj.loss_and_gradient(12, target, 0.5)
+    assert L > 0
+    # Probe cells (0, 0) and (1, 4) are paced; (3, 2) is a probe at rest;
+    # (2, 2) is no probe (the model has no diffusion current)
+    for idx in ((0, 0), (4, 1), (2, 3), (2, 2)):
+        h = 1e-4 * f0[idx]
+        vals = []
+        for sgn in (1, -1):
+            f = f0.copy()
+            f[idx] += sgn * h
+            s.set_field('ina.gNa', f)
+            vals.append(_loss(s, adj, target))
+        s.set_field('ina.gNa', f0)
+        fd = (vals[0] - vals[1]) / (2 * h)
+        ad = grads['ina.gNa'][idx]
+        assert abs(ad - fd) <= 1e-4 * max(abs(fd), 1e-6 * L), (idx, ad, fd)
