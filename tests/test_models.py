@@ -7,8 +7,8 @@ Every cell model in myokit's test data through both implementations.
   (``myokit/_sim/openclsim.py:195-260``); every accepted model's generated
   kernel compiles with NVRTC in double precision with forward Euler and in
   single precision with Rush-Larsen.
-- GPU: every accepted model on a small paced sheet, every state and bound
-  variable of every cell logged, against the oracle in double precision
+- GPU: every accepted model on a small paced sheet, every state,
+  intermediary (double precision) and bound variable of every cell logged, against the oracle in double precision
   (forward Euler and Rush-Larsen; with and without diffusion; bar 1e-9
   relative, observed at most 1.4e-13) and in single precision (bar 1e-3
   relative, observed at most 1.5e-4).
@@ -31,6 +31,8 @@ from oracle.refsim import ReferenceCpuSimulation
 
 DP = myokit.DOUBLE_PRECISION
 SP = myokit.SINGLE_PRECISION
+# Everything SimulationOpenCL can log: states, intermediaries, bound
+LOG = myokit.LOG_STATE + myokit.LOG_INTER + myokit.LOG_BOUND
 
 FILES = sorted(f for f in os.listdir(DATA) if f.endswith('.mmt'))
 LABELLED = ['beeler-1977-units.mmt', 'lr-1991-dep.mmt', 'conditional.mmt']
@@ -78,7 +80,7 @@ def test_kernels_compile(name):
         assert len(cubin) > 0
 
 
-def _run(cls, m, prec, rl, diffusion=True):
+def _run(cls, m, prec, rl, diffusion=True, log=LOG):
     # Half the sheet paced, so that the models fire and (where they have a
     # diffusion current) the wave crosses the other half within 30 ms.
     # Without diffusion every cell is paced.
@@ -87,7 +89,7 @@ def _run(cls, m, prec, rl, diffusion=True):
     if diffusion:
         s.set_paced_cells(3, 3)
         s.set_conductance(2, 2)
-    return s.run(30, log_interval=0.25)
+    return s.run(30, log=log, log_interval=0.25)
 
 
 def _worst(a, b):
@@ -109,7 +111,13 @@ def _worst(a, b):
     (DP, False, False, 1e-9)],
     ids=['fp64', 'fp64-rl', 'fp32-rl', 'fp64-no-diffusion'])
 def test_model_parity(name, prec, rl, diffusion, tol):
+    # Single precision: states and bound variables. Some intermediaries
+    # lose most of their digits in single precision, in both implementations
+    # alike: Decker 2009's ical.zz = (0.003 / Ca_cal)^4, with Ca_cal from a
+    # cubic-root formula that cancels, differs by 0.47 of its maximum. They
+    # are compared in double precision.
     m = _model(name)
-    ref = _run(ReferenceCpuSimulation, m, prec, rl, diffusion)
-    out = _run(mg.SimulationCUDA, m, prec, rl, diffusion)
+    log = LOG if prec == DP else myokit.LOG_STATE + myokit.LOG_BOUND
+    ref = _run(ReferenceCpuSimulation, m, prec, rl, diffusion, log)
+    out = _run(mg.SimulationCUDA, m, prec, rl, diffusion, log)
     assert _worst(ref, out) <= tol
