@@ -105,6 +105,9 @@ def parse():
     p.add_argument('--accumulate', choices=['none', 'kahan', 'double'],
                    default='none')
     p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--clocks-csv', default=None,
+                   help='also write the raw nvidia-smi clock samples of the'
+                        ' timed region to this CSV file')
     p.add_argument('--cpu-seconds', type=float, default=12.0,
                    help='target CPU work for the cpu_baseline sample')
     return p.parse_args()
@@ -804,9 +807,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         logs32.append(s.run(args.step_ms, log=log, log_interval=1))
     kernel = s._last_kernel
-    sampler = ClockSampler(os.path.join(ROOT, 'gpurun_out', 'clocks.csv')
-                           if os.path.isdir(os.path.join(ROOT, 'gpurun_out'))
-                           else None)
+    sampler = ClockSampler(args.clocks_csv)
     sampler.start()
     barrier()
     dev_ms = 0.0
