@@ -84,7 +84,11 @@ typedef struct mkg_config {
     int32_t n_hi;           /* number of selected states (mkg_set_hi_states) */
     int32_t stage;          /* 1: the kernel copies each warp tile's inputs
                                into shared memory with TMA tensor copies and
-                               takes the tensor maps as a second parameter */
+                               takes the tensor maps as a second parameter;
+                               2: the same with two buffers per warp (the
+                               copies of the tile after the next run while
+                               a tile computes); the dynamic shared memory
+                               per CTA is warps x stage x bytes + 128 */
     int32_t v_double;       /* 1: V is stored and updated in FP64 (hi_mode 1
                                with V among the selected states) */
 } mkg_config;

@@ -18,13 +18,15 @@ import numpy as np
 
 from ._deps import myokit
 
-# Candidate (threads per CTA, min CTAs per SM, steps per launch, lazy tile
+# Candidate (threads per CTA, min CTAs per SM, steps per launch, tile
 # staging, step synchronisation). The register cap is 64K / (threads * min
 # CTAs), and a warp scheduler holds 16K registers. 576 and 640 threads trade
 # registers for the 18 or 20 warps per SM that even out the warp tiles of
-# mid-size sheets; lazy staging (values read from shared memory where used)
-# keeps those kernels from spilling. Steps are separated by a grid barrier
-# or by waits on the neighbouring warps only.
+# mid-size sheets. Staging 0 prefetches each tile into registers; 1 and 2
+# read it from shared memory where used (lazy), which keeps those kernels
+# from spilling, with one or two buffers per warp (2: the copies of the
+# tile after the next overlap a tile's computation). Steps are separated by
+# a grid barrier or by waits on the neighbouring warps only.
 _B, _N = 'barrier', 'neighbors'
 _CANDIDATES = [
     ((256, 1), 2, 0, False, _B), ((128, 1), 4, 0, False, _B),
@@ -37,6 +39,7 @@ _CANDIDATES = [
     ((512, 1), 1, 0, False, _N), ((384, 1), 1, 0, False, _N),
     ((256, 1), 2, 0, False, _N), ((640, 1), 1, 0, True, _N),
     ((256, 1), 2, 0, True, _N),
+    ((256, 1), 2, 0, 2, _B), ((384, 1), 1, 0, 2, _N),
 ]
 _CANDIDATES_FP64 = [((128, 1), 1, 0, False, _B), ((256, 1), 1, 0, False, _B),
                     ((64, 1), 1, 0, False, _B), ((32, 1), 1, 0, False, _B),
@@ -87,7 +90,7 @@ def _apply(sim, block, min_blocks, spl, lazy=False, sync='barrier'):
     sim._block = tuple(block)
     sim._min_blocks = int(min_blocks)
     sim._steps_per_launch = int(spl)
-    sim._stage_lazy = bool(lazy)
+    sim._stage_lazy = int(lazy)
     sim._sync = sync
     sim._graphs = 1
 
@@ -149,7 +152,7 @@ def autotune(sim, duration=None, candidates=None, store=True,
         d[signature(sim)] = {
             'block': list(best[0]), 'min_blocks': best[1],
             'steps_per_launch': best[2],
-            'stage_lazy': bool(best[3]) if len(best) > 3 else False,
+            'stage_lazy': int(best[3]) if len(best) > 3 else 0,
             'sync': best[4] if len(best) > 4 else 'barrier',
             'rate': results[best],
             'when': time.strftime('%Y-%m-%dT%H:%M:%S')}

@@ -784,6 +784,8 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
         return set_err(nullptr, MKG_ERR_ARG, "2D diffusion needs two_d");
     if (cfg->v_double && cfg->hi_mode != MKG_HI_DOUBLE)
         return set_err(nullptr, MKG_ERR_ARG, "v_double needs hi_mode 1");
+    if (cfg->stage < 0 || cfg->stage > 2)
+        return set_err(nullptr, MKG_ERR_ARG, "stage must be 0, 1 or 2");
     if (cfg->stage) {
         /* Tensor copy limits: 256 planes per box, int32 coordinates */
         StageLayout L;
@@ -822,8 +824,10 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
                                cfg->device));
     if (cfg->stage) {
         compute_stage_layout(cfg, &s->lay);
-        /* + 128: the kernel rounds the base up to a 128-byte boundary */
-        s->tile_smem = (size_t)(cfg->block_x / 32) * s->lay.bytes + 128;
+        /* One or two buffers per warp (cfg.stage); + 128: the kernel
+         * rounds the base up to a 128-byte boundary */
+        s->tile_smem = (size_t)(cfg->block_x / 32) * s->lay.bytes *
+                           (size_t)cfg->stage + 128;
         CKC(cudaKernelSetAttributeForDevice(
             s->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
             (int)s->tile_smem, cfg->device));

@@ -384,9 +384,12 @@ class TissueKernel(object):
         step counters). Connection graphs always use the barrier.
     ``stage_lazy``
         With staging: read staged values from shared memory where they are
-        used and start the next tile's copies after the computation, instead
-        of reading them all into registers first and copying ahead. Needs
-        fewer registers, so more warps fit on an SM.
+        used, instead of reading them all into registers first and copying
+        the next tile ahead. Needs fewer registers, so more warps fit on an
+        SM. ``1`` (or True): one buffer per warp, the next tile's copies
+        start after the computation; ``2``: two buffers per warp, the tile
+        after the next is copied while a tile computes (twice the shared
+        memory).
     """
     def __init__(self, model, precision, native_math, bound_variables,
                  inter_log, diffusion, two_d, fields, rl_states, block,
@@ -434,7 +437,9 @@ class TissueKernel(object):
         self.traj = bool(traj)
         self.stage = bool(stage)
         self.row_pad = bool(row_pad) and self.two_d
-        self.stage_lazy = bool(stage_lazy)
+        self.stage_lazy = int(stage_lazy)
+        if self.stage_lazy not in (0, 1, 2):
+            raise ValueError('stage_lazy must be 0, 1 or 2')
         if sync not in ('barrier', 'neighbors'):
             raise ValueError('sync must be "barrier" or "neighbors"')
         # Connection graphs have arbitrary neighbours: grid barrier only
@@ -452,10 +457,16 @@ class TissueKernel(object):
                 8 if self.v_double else real, v_rows,
                 self.diffusion == DIFF_HETERO and not self.two_d,
                 bool(row_pad) and self.two_d)
+            per_cta = lay['bytes'] * (self.block[0] // 32)
             if (max(lay['np'], len(self.hi_states), len(self.fields))
-                    <= STAGE_MAX_BOX and
-                    lay['bytes'] * (self.block[0] // 32) <= STAGE_MAX_CTA):
+                    <= STAGE_MAX_BOX and per_cta <= STAGE_MAX_CTA):
                 self.layout = lay
+                # Two buffers per warp only where they fit
+                if self.stage_lazy == 2 and 2 * per_cta > STAGE_MAX_CTA:
+                    self.stage_lazy = 1
+        # Staging buffers per warp (mkg_config.stage)
+        self.stage_buffers = 2 if self.layout and self.stage_lazy == 2 \
+            else 1
         self.census = OpCensus()
         self._source = self._generate()
 
@@ -753,6 +764,8 @@ class TissueKernel(object):
             '@NBR_SYNC@': '1' if self.sync == 'neighbors' else '0',
             '@STAGE@': '1' if self.layout else '0',
             '@STAGE_LAZY@': '1' if self.layout and self.stage_lazy else '0',
+            '@STAGE_BUFS@': '2' if self.layout and self.stage_lazy == 2
+            else '1',
             '@SW@': str(lay.get('sw', 32)),
             '@VW@': str(STAGE_VW),
             '@ST_LO@': str(lay.get('lo', 0)),

@@ -776,14 +776,15 @@ class SimulationCUDA(object):
         return 'barrier'
 
     def _lazy_staging(self):
-        """Staged tiles read where used (True) or prefetched (False)."""
+        """Staged tiles prefetched into registers (0), or read where used
+        from one (1) or two (2) shared-memory buffers per warp."""
         if self._stage_lazy is not None:
-            return self._stage_lazy
+            return int(self._stage_lazy)
         if self._block is None:
             hit = self._tuned_choice()
             if hit is not None:
-                return bool(hit.get('stage_lazy', False))
-        return False
+                return int(hit.get('stage_lazy', 0))
+        return 0
 
     def _block_shape(self, two_d):
         """CTA shape (threads, 1); threads is a multiple of the warp size."""
@@ -907,7 +908,7 @@ class SimulationCUDA(object):
         cfg.hi_mode = {None: 0, 'double': 1, 'kahan': 2}[kernel.accumulate] \
             if kernel.hi_states else 0
         cfg.n_hi = len(kernel.hi_states)
-        cfg.stage = 1 if kernel.layout else 0
+        cfg.stage = kernel.stage_buffers if kernel.layout else 0
         cfg.v_double = 1 if kernel.v_double else 0
         key = (kernel.key(), bytes(cfg))
         if self._backend is not None and self._backend[0] == key:

@@ -75,6 +75,26 @@ def test_kernels_stage_only_large_grids(br77):
     assert s._kernel([]).layout is None
 
 
+def test_two_buffer_staging_compiles_and_falls_back(decker):
+    # Two buffers per warp where they fit (the CTA's staging memory under
+    # the cap), one otherwise; the host sizes shared memory from the
+    # simulation's configuration (mkg_config.stage = buffers)
+    for block, bufs in ((256, 2), (640, 1)):
+        s = mg.SimulationCUDA(decker, None, ncells=(64, 32), rl=True,
+                              block=block, min_blocks=1)
+        s._stage_lazy = 2
+        k = s._kernel([])
+        assert k.layout is not None and k.stage_buffers == bufs
+        assert ('#define STAGE_BUFS %d' % bufs) in k.source()
+        assert k.stage_lazy == bufs
+        cubin, _ = _lib.compile_source(k.source(), k.options())
+        assert cubin[:4] == b'\x7fELF'
+    with pytest.raises(ValueError):
+        exporter.TissueKernel(
+            decker, myokit.SINGLE_PRECISION, False, {}, [], 0, False, [], {},
+            (256, 1), stage=True, stage_lazy=3)
+
+
 # ---------------------------------------------------------------------------
 # GPU
 # ---------------------------------------------------------------------------
@@ -82,7 +102,7 @@ def test_kernels_stage_only_large_grids(br77):
 def _run(model, stage, ncells, precision=SP, rl=False, fields=None,
          gfield=None, conn=None, diffusion=True, dur=4.0, **kw):
     p = myokit.pacing.blocktrain(period=1000, duration=2, offset=0.5)
-    lazy = stage == 'lazy'
+    lazy = {'lazy': 1, 'lazy2': 2}.get(stage, 0)
     s = mg.SimulationCUDA(model, p, ncells=ncells, precision=precision,
                           rl=rl, diffusion=diffusion, stage_tiles=bool(stage),
                           **kw)
@@ -141,9 +161,10 @@ def test_staged_equals_direct_grid(decker, shape, precision):
     sh = shape[::-1] if isinstance(shape, tuple) else shape
     f = _fields(decker, sh, ['ikr.Gbar', 'ina.Gbar'])
     out = [_run(decker, st, shape, precision, rl=True, fields=f)
-           for st in (False, True, 'lazy')]
+           for st in (False, True, 'lazy', 'lazy2')]
     _same(out[0], out[1])
     _close(out[0], out[2], 1e-3 if precision == SP else 1e-9)
+    _close(out[0], out[3], 1e-3 if precision == SP else 1e-9)
 
 
 @pytest.mark.gpu
@@ -152,9 +173,10 @@ def test_staged_equals_direct_grid(decker, shape, precision):
 def test_staged_equals_direct_accumulate(decker, acc, shape):
     f = _fields(decker, shape[::-1], ['ikr.Gbar'])
     out = [_run(decker, st, shape, SP, rl=True, fields=f, accumulate=acc)
-           for st in (False, True, 'lazy')]
+           for st in (False, True, 'lazy', 'lazy2')]
     _same(out[0], out[1])
     _close(out[0], out[2], 1e-3)
+    _close(out[0], out[3], 1e-3)
 
 
 @pytest.mark.gpu
@@ -216,7 +238,7 @@ def test_staged_matches_oracle_fp64(br77, shape):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('stage', [False, True, 'lazy'])
+@pytest.mark.parametrize('stage', [False, True, 'lazy', 'lazy2'])
 @pytest.mark.parametrize('shape', [(64, 20), (37, 23), 1000, (2000, 1),
                                    (3, 400), 300])
 def test_neighbour_sync_equals_grid_barrier(decker, stage, shape):
@@ -228,7 +250,7 @@ def test_neighbour_sync_equals_grid_barrier(decker, stage, shape):
         s = mg.SimulationCUDA(decker, p, ncells=shape, rl=True,
                               stage_tiles=bool(stage), block=64,
                               min_blocks=1)
-        s._stage_lazy = stage == 'lazy'
+        s._stage_lazy = {'lazy': 1, 'lazy2': 2}.get(stage, 0)
         s._sync = sync
         if isinstance(shape, tuple):
             s.set_paced_cells(3, shape[1])
