@@ -63,9 +63,10 @@ def parse():
     p.add_argument('--accuracy-ms', type=float, default=400.0,
                    help='simulated time of the precision comparison runs'
                         ' (0 = skip)')
-    p.add_argument('--adjoint-ms', type=float, default=100.0,
-                   help='simulated time of the adjoint measurement'
-                        ' (0 = skip)')
+    p.add_argument('--adjoint-ms', type=float, default=300.0,
+                   help='simulated time of the adjoint measurement (the'
+                        ' 256 x 256 adjoint configuration runs 300 ms;'
+                        ' 0 = skip)')
     p.add_argument('--configs', default='c1,c3,c5',
                    help='other configurations to time: comma list of c1'
                         ' (200-cell FP64 cable), c3 (512 batched cables), c5'
