@@ -108,10 +108,10 @@ int mkg_stage_layout(const mkg_config *cfg, int64_t *out);
  * waits on neighbouring warps between steps, and the tile-copy waits) to
  * timeout_ns (1 ms .. 60 s; default 2 s). A wait that runs out records
  * MKG_DEV_TIMEOUT, every block leaves the kernel, and mkg_run_chunk returns
- * MKG_ERR_TIMEOUT with the context still usable. skew > 0 raises the target
- * of every step wait so that it cannot be reached: a way to exercise that
- * path from the host (0 restores normal runs). No counterpart in the
- * reference.
+ * MKG_ERR_TIMEOUT with the context still usable. skew (0 .. 65536) > 0
+ * raises the target of every step wait so that it cannot be reached: a way
+ * to exercise that path from the host (0 restores normal runs). No
+ * counterpart in the reference.
  */
 int mkg_set_wait(mkg_sim *sim, int64_t timeout_ns, int32_t skew);
 

@@ -1199,6 +1199,15 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
     if (!s->running)
         return set_err(s, MKG_ERR_ORDER, "mkg_run_chunk before mkg_run_begin");
     if (max_steps < 1) return set_err(s, MKG_ERR_ARG, "max_steps < 1");
+    {
+        /* The grid barrier counts (steps + skew) x CTAs arrivals per chunk
+         * in the low 31 bits of its counter (the top bit carries a NaN
+         * halt): a chunk is kept short enough not to overflow it */
+        const int64_t ctas = std::max<int64_t>(
+            1, (int64_t)s->occ_blocks * (int64_t)s->num_sms);
+        const int64_t cap = (int64_t)0x7fffffff / ctas - 2 - s->wait_skew;
+        max_steps = std::min<int64_t>(max_steps, std::max<int64_t>(cap, 1));
+    }
     s->last_ms = 0;
     s->last_launches = 0;
     s->last_cell_steps = 0;
@@ -1493,9 +1502,11 @@ int mkg_last_stats(const mkg_sim *s, double *kernel_ms, int64_t *launches,
 int mkg_set_wait(mkg_sim *s, int64_t timeout_ns, int32_t skew)
 {
     if (!s) return set_err(s, MKG_ERR_ARG, "null argument");
-    if (timeout_ns < 1000000 || timeout_ns > 60000000000LL || skew < 0)
+    if (timeout_ns < 1000000 || timeout_ns > 60000000000LL || skew < 0 ||
+        skew > 65536)
         return set_err(s, MKG_ERR_ARG,
-                       "the wait bound must be 1 ms to 60 s, the skew >= 0");
+                       "the wait bound must be 1 ms to 60 s, the skew 0 to"
+                       " 65536");
     clear_graphs(s);
     s->timeout_ns = timeout_ns;
     s->wait_skew = skew;

@@ -55,5 +55,6 @@ def test_wait_bound_is_checked(decker):
     s = _sim(decker, 'barrier', False)
     s.run(0.1)
     be = s._backend[1]
-    for bad in ((0, 0), (10 ** 12, 0), (2000000000, -1)):
+    for bad in ((0, 0), (10 ** 12, 0), (2000000000, -1),
+                (2000000000, 65537)):
         assert be.lib.mkg_set_wait(be.h, *bad) == _lib.MKG_ERR_ARG
