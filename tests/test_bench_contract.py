@@ -37,3 +37,20 @@ def test_help_lists_options():
     for opt in ('--gpus', '--steps', '--warmup', '--impl', '--tune',
                 '--profile', '--configs'):
         assert opt in r.stdout
+
+
+def test_reference_arm_under_torchrun_two_ranks():
+    # Launched like the multi-GPU runs: rank 0 alone runs and prints one
+    # line, the other rank exits 0 without work
+    r = subprocess.run(
+        [sys.executable, '-m', 'torch.distributed.run', '--nnodes=1',
+         '--nproc-per-node', '2', '--master-addr', '127.0.0.1',
+         '--master-port', '29533', os.path.join(ROOT, 'bench.py'),
+         '--impl', 'reference', '--size', '16', '--steps', '1', '--warmup',
+         '1', '--gpus', '2'],
+        capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.strip().splitlines() if ln.startswith('{')]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line['impl'] == 'reference' and line['value'] > 0
