@@ -211,3 +211,66 @@ def frames_to_block(times, frames, name='membrane.V'):
     block = myokit.DataBlock2d(nx, ny, np.asarray(times, dtype=float))
     block.set2d(name, data)
     return block
+
+
+_README_FRAMES = (
+    'Frames recorded on the device by myokit_gb300, in the file format of\n'
+    'myokit.DataBlock{d}d.save: header_block{d}d.txt holds nt, {dims}the\n'
+    'data type and the entry names; data.bin holds little-endian doubles:\n'
+    'the nt times, then each {d}d entry in C order.\n')
+
+
+def save_frames(path, times, frames, name='membrane.V', chunk=16):
+    """
+    Writes device frames (as returned by :meth:`SimulationCUDA.run_frames`)
+    to ``path`` in the file format of ``myokit.DataBlock2d.save`` (frames
+    shaped ``(n, ny, nx)``) or ``myokit.DataBlock1d.save`` (``(n, nx)``),
+    ``myokit/_datablock.py:1423-1500, 631-704``: a zip archive holding a
+    text header, ``data.bin`` (little-endian doubles: the times, then every
+    entry in C order) and a readme. The frames are copied to the host
+    ``chunk`` at a time and streamed into the archive, so the host never
+    holds the whole block; ``myokit.DataBlock2d.load`` (or ``1d``) reads the
+    file. ``frames`` is one tensor or array, stored as ``name``, or a dict
+    ``{name: frames}`` of equally shaped frame sets.
+    """
+    import os
+    import zipfile
+    sets = dict(frames) if isinstance(frames, dict) else {name: frames}
+    if not sets:
+        raise ValueError('No frames to save.')
+    t = np.ascontiguousarray(times, dtype='<f8')
+    shape = None
+    for k, f in sets.items():
+        s = tuple(f.shape)
+        if len(s) not in (2, 3):
+            raise ValueError('Frames are shaped (n, nx) or (n, ny, nx).')
+        if shape is not None and s != shape:
+            raise ValueError('Every frame set must have the same shape.')
+        shape = s
+    if shape[0] != len(t):
+        raise ValueError('One time per frame is needed.')
+    chunk = max(1, int(chunk))
+    d = len(shape) - 1
+    head = [str(shape[0])] + [str(x) for x in shape[1:]] + ['"d"', str(d)]
+    head += ['"%s"' % k for k in sets]
+
+    def host(f, i, j):
+        # Frames i..j-1 as host doubles (torch tensors on any device, or
+        # arrays)
+        if hasattr(f, 'detach'):
+            import torch
+            return f[i:j].detach().to('cpu', torch.float64).numpy()
+        return np.asarray(f[i:j], dtype=np.float64)
+
+    with zipfile.ZipFile(os.path.expanduser(path), 'w',
+                         compression=zipfile.ZIP_DEFLATED,
+                         allowZip64=True) as z:
+        z.writestr('header_block%dd.txt' % d, '\n'.join(head))
+        with z.open('data.bin', 'w', force_zip64=True) as out:
+            out.write(t.tobytes())
+            for f in sets.values():
+                for i in range(0, shape[0], chunk):
+                    block = host(f, i, min(shape[0], i + chunk))
+                    out.write(np.ascontiguousarray(block, '<f8').tobytes())
+        dims = 'ny, nx, ' if d == 2 else 'nx, '
+        z.writestr('readme.txt', _README_FRAMES.format(d=d, dims=dims))
