@@ -69,3 +69,95 @@ def compare(t, traces, reference):
             n_apd += 1
     return {'max_abs_dV_mV': dv, 'max_activation_error_ms': dta,
             'max_apd90_error_ms': dapd, 'traces_with_apd90': n_apd}
+
+
+def _frames64(frames):
+    import torch
+    f = frames if torch.is_tensor(frames) else torch.as_tensor(
+        np.asarray(frames, dtype=float))
+    return f.detach().to(torch.float64)
+
+
+def _first(mask):
+    """Index of the first True along dim 0, and whether there is one."""
+    import torch
+    has = mask.any(dim=0)
+    return torch.argmax(mask.to(torch.int8), dim=0), has
+
+
+def _at(x, idx):
+    return x.gather(0, idx.unsqueeze(0)).squeeze(0)
+
+
+def activation_map(times, frames, threshold=-30.0):
+    """
+    :func:`activation_time` of every cell of a frame set at once: ``frames``
+    shaped ``(n, ...)`` (a torch tensor on any device, as returned by
+    ``SimulationCUDA.run_frames``, or an array), ``times`` the ``n`` frame
+    times. Returns a float64 tensor shaped like one frame, on the frames'
+    device, NaN where V never crosses ``threshold`` upwards.
+    """
+    import torch
+    v = _frames64(frames)
+    t = torch.as_tensor(np.asarray(times, dtype=float), device=v.device)
+    if v.shape[0] != t.shape[0] or v.shape[0] < 2:
+        raise ValueError('One time per frame, and at least two frames.')
+    above = v >= threshold
+    i, has = _first(above[1:] & ~above[:-1])
+    vi, vj = _at(v, i), _at(v, i + 1)
+    ti, tj = t[i], t[i + 1]
+    ta = ti + (threshold - vi) / (vj - vi) * (tj - ti)
+    return torch.where(has, ta, torch.full_like(ta, float('nan')))
+
+
+def apd90_map(times, frames, threshold=-30.0):
+    """
+    :func:`apd90` of every cell of a frame set at once (see
+    :func:`activation_map`): from activation until V first falls below
+    ``V_rest + 0.1 * (V_peak - V_rest)`` after the peak, V_rest the first
+    frame's value. NaN where there is no activation or no repolarisation.
+    """
+    import torch
+    v = _frames64(frames)
+    t = torch.as_tensor(np.asarray(times, dtype=float), device=v.device)
+    ta = activation_map(times, v, threshold)
+    n = v.shape[0]
+    k = torch.arange(n, device=v.device).reshape((n,) + (1,) * (v.dim() - 1))
+    # First frame at or after the activation time, then the peak from there
+    i0 = (t.reshape(k.shape) < ta.unsqueeze(0)).sum(dim=0)
+    masked = torch.where(k >= i0.unsqueeze(0), v,
+                         torch.full_like(v, float('-inf')))
+    ip = torch.argmax(masked, dim=0)
+    vrest = v[0]
+    level = vrest + 0.1 * (_at(v, ip) - vrest)
+    j, has = _first((v < level.unsqueeze(0)) & (k >= ip.unsqueeze(0)))
+    jm = (j - 1).clamp(min=0)
+    vj, vm = _at(v, j), _at(v, jm)
+    tr = t[jm] + (level - vm) / (vj - vm) * (t[j] - t[jm])
+    ok = has & torch.isfinite(ta)
+    return torch.where(ok, tr - ta, torch.full_like(ta, float('nan')))
+
+
+def compare_frames(times, frames, reference, threshold=-30.0):
+    """
+    :func:`compare` over every cell of two frame sets (for example the
+    single- and double-precision ``run_frames`` of one simulation), computed
+    on the frames' device: ``max_abs_dV_mV``, ``max_activation_error_ms``
+    and ``max_apd90_error_ms`` (where both are defined), and
+    ``cells_with_apd90``.
+    """
+    import torch
+    a = _frames64(frames)
+    b = _frames64(reference).to(a.device)
+    if a.shape != b.shape:
+        raise ValueError('The frame sets must have the same shape.')
+    dv = float((a - b).abs().max())
+    ta, tb = activation_map(times, a, threshold), activation_map(
+        times, b, threshold)
+    both = torch.isfinite(ta) & torch.isfinite(tb)
+    dta = float((ta - tb).abs()[both].max()) if bool(both.any()) else 0.0
+    pa, pb = apd90_map(times, a, threshold), apd90_map(times, b, threshold)
+    both = torch.isfinite(pa) & torch.isfinite(pb)
+    dp = float((pa - pb).abs()[both].max()) if bool(both.any()) else 0.0
+    return {'max_abs_dV_mV': dv, 'max_activation_error_ms': dta,
+            'max_apd90_error_ms': dp, 'cells_with_apd90': int(both.sum())}
