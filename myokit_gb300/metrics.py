@@ -161,3 +161,64 @@ def compare_frames(times, frames, reference, threshold=-30.0):
     dp = float((pa - pb).abs()[both].max()) if bool(both.any()) else 0.0
     return {'max_abs_dV_mV': dv, 'max_activation_error_ms': dta,
             'max_apd90_error_ms': dp, 'cells_with_apd90': int(both.sum())}
+
+
+def cable_cv(times, frames, threshold=-30, length=0.01, time_multiplier=1e-3,
+             border=None):
+    """
+    Conduction velocity (cm/s) of a cable from frames shaped ``(n, nx)`` (a
+    torch tensor on any device, or an array), as ``myokit.DataBlock1d.cv``
+    computes it from a block (``myokit/_datablock.py:152-248``), with the
+    same arguments and rules: per cell, the first frame after the first
+    where V exceeds -30 mV while rising (the reference's fixed detection
+    level), interpolated linearly to ``threshold``; cells from the first
+    with a crossing to the last of the run that follows, ``border`` cells
+    left out at each end (default a third, at most 50); a least-squares
+    line through (time, position). Returns 0 without a crossing. The
+    crossings are found on the frames' device; only one time per cell
+    comes to the host.
+    """
+    import torch
+    v = _frames64(frames)
+    if v.dim() != 2:
+        raise ValueError('Cable frames are shaped (n, nx).')
+    n, nx = v.shape
+    if border is None:
+        border = min(50, nx // 3)
+    else:
+        border = int(border)
+        if border < 0:
+            raise ValueError('The argument `border` cannot be negative.')
+        elif border >= nx // 2:
+            raise ValueError(
+                'The argument `border` must be less than half the number'
+                ' of cells.')
+    t = np.asarray(times, dtype=float)
+    # Per cell: first frame k >= 1 with V_k > -30 and V_k > V_(k-1)
+    rise = (v[1:] > -30) & (v[1:] - v[:-1] > 0)
+    k, has = _first(rise)
+    k = k + 1
+    v1 = _at(v, k)
+    v0 = _at(v, k - 1)
+    k = k.cpu().numpy()
+    has = has.cpu().numpy() & (k > 1)
+    v0, v1 = v0.cpu().numpy(), v1.cpu().numpy()
+    ts, i1, i2 = [], None, None
+    for i in range(border, nx - border):
+        if not has[i]:
+            if i1 is not None:
+                i2 = i - 1
+                break
+            continue
+        if i1 is None:
+            i1 = i
+        else:
+            i2 = i
+        t0, t1 = t[k[i] - 1], t[k[i]]
+        ts.append(t0 + (threshold - v0[i]) * (t1 - t0) / (v1[i] - v0[i]))
+    if i1 is None:
+        return 0
+    ts = np.asarray(ts) * time_multiplier
+    x = np.arange(i1, 1 + i2, dtype=float) * length
+    a = np.vstack([ts, np.ones(len(ts))]).T
+    return np.linalg.lstsq(a, x, rcond=None)[0][0]

@@ -67,3 +67,41 @@ def test_frame_metric_argument_checks():
     with pytest.raises(ValueError, match='same shape'):
         metrics.compare_frames(np.arange(3.0), np.zeros((3, 2)),
                                np.zeros((3, 3)))
+
+
+@pytest.fixture(scope='module')
+def cable_block():
+    # A paced 80-cell Beeler-Reuter cable run by the oracle (the reference
+    # SimulationOpenCL on its CPU backend), as a reference DataBlock1d
+    from conftest import load, myokit
+    from oracle.refsim import ReferenceCpuSimulation
+    m = load('beeler-1977-model.mmt')
+    m.get('membrane.i_stim.amplitude').set_rhs(-80)
+    p = myokit.pacing.blocktrain(period=1000, duration=2, offset=1)
+    s = ReferenceCpuSimulation(m, p, ncells=80,
+                               precision=myokit.DOUBLE_PRECISION)
+    s.set_paced_cells(3)
+    d = s.run(30, log=['engine.time', 'membrane.V'], log_interval=0.25)
+    return myokit.DataBlock1d.from_log(d)
+
+
+@pytest.mark.parametrize('kw', [{}, {'threshold': -20, 'border': 5},
+                                {'length': 0.02, 'border': 0}])
+def test_cable_cv_equals_reference(cable_block, kw):
+    t = cable_block.time()
+    v = cable_block.get1d('membrane.V')
+    ref = cable_block.cv('membrane.V', **kw)
+    got = metrics.cable_cv(t, torch.tensor(v, dtype=torch.float64), **kw)
+    assert ref > 0 and got == ref
+
+
+def test_cable_cv_edge_cases():
+    t = np.arange(10.0)
+    flat = np.full((10, 12), -85.0)
+    assert metrics.cable_cv(t, flat) == 0
+    with pytest.raises(ValueError, match='negative'):
+        metrics.cable_cv(t, flat, border=-1)
+    with pytest.raises(ValueError, match='less than half'):
+        metrics.cable_cv(t, flat, border=6)
+    with pytest.raises(ValueError, match='shaped'):
+        metrics.cable_cv(t, np.zeros((10, 2, 2)))
