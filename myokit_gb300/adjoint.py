@@ -323,16 +323,8 @@ class AdjointKernel(object):
         loss_target = A(name(states[fwd.i_vm])) if fwd.i_vm >= 0 else \
             A(name(fwd.vm))
         subs = {
-            '@REAL@': 'float' if self.single else 'double',
-            '@N_STATE@': str(fwd.n_state),
-            '@N_FIELD@': str(len(fwd.fields)),
-            '@I_VM@': str(max(fwd.i_vm, 0)),
-            '@DIFF@': str(fwd.diffusion),
-            '@TWO_D@': '1' if fwd.two_d else '0',
-            '@BX@': str(fwd.block[0]),
             '@ADJ_MINB@': str(self.min_blocks),
             '@ADJ_BX@': str(self.threads),
-            '@POW_HELPERS@': _exp._pow_helpers(self.single),
             '@FORWARD@': '\n'.join(fw),
             '@SEEDS@': '\n'.join(seeds),
             '@LOSS_TARGET@': loss_target,
@@ -347,8 +339,8 @@ class AdjointKernel(object):
 
     @staticmethod
     def _join(fsrc, text):
-        """Appends the adjoint kernel to the forward module, dropping the
-        definitions both templates share."""
+        """Appends the adjoint kernel (the template from its declaration
+        on) to the forward module, which defines what it uses."""
         start = text.index('extern "C" __global__')
         return fsrc + '\n' + text[start:]
 
