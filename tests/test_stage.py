@@ -95,6 +95,32 @@ def test_two_buffer_staging_compiles_and_falls_back(decker):
             (256, 1), stage=True, stage_lazy=3)
 
 
+@pytest.mark.parametrize('mode', [
+    (SP, None), (SP, 'kahan'), (SP, 'double'), (myokit.DOUBLE_PRECISION,
+                                                 None)],
+    ids=['fp32', 'kahan', 'double', 'fp64'])
+def test_every_staging_and_sync_mode_compiles(br77, mode):
+    # Direct loads, prefetch, lazy with one or two buffers, each with the
+    # grid barrier and with neighbour waits, 2D and 1D heterogeneous
+    precision, acc = mode
+    for ncells, hetero in (((48, 12), False), (600, True)):
+        for lazy in (None, 0, 1, 2):
+            for sync in ('barrier', 'neighbors'):
+                s = mg.SimulationCUDA(br77, None, ncells=ncells, rl=True,
+                                      precision=precision, accumulate=acc,
+                                      stage_tiles=lazy is not None,
+                                      block=128, min_blocks=1)
+                s._stage_lazy = lazy or 0
+                s._sync = sync
+                if hetero:
+                    s.set_conductance_field(np.full(599, 2.0), None)
+                k = s._kernel([])
+                assert (k.layout is not None) == (lazy is not None)
+                assert k.sync == sync
+                cubin, _ = _lib.compile_source(k.source(), k.options())
+                assert cubin[:4] == b'\x7fELF'
+
+
 # ---------------------------------------------------------------------------
 # GPU
 # ---------------------------------------------------------------------------
