@@ -174,13 +174,14 @@ int mkg_get_state(mkg_sim *sim, double *state, int64_t n);
  * clCreateBuffer per run).
  *
  * mkg_set_state stages the doubles in a device buffer that the handle
- * allocates with cudaMalloc the first time. Callers that cannot call
- * cudaMalloc at the point where they upload a state -- while a stream is
- * being captured into a CUDA graph, or in a real-time pacing loop that
- * must not suffer cudaMalloc's device-wide synchronisation -- use this call:
- * it stages through a fixed 16 MiB array in the library's device image
- * (held on every GPU that loads the library until the process exits) and
- * calls no cudaMalloc, cudaFree or other allocating routine.
+ * allocates with cudaMalloc the first time. Some callers must not call
+ * cudaMalloc where they upload a state: a host loop that paces a tissue in
+ * real time (cudaMalloc can synchronise the whole device and stall every
+ * stream), or a host that keeps device memory in its own pool or under a
+ * fixed budget (a cudaMalloc outside that pool can fail). They use this
+ * call: it stages through a fixed 16 MiB array in the library's device
+ * image (held on every GPU that loads the library until the process exits)
+ * and calls no cudaMalloc, cudaFree or other allocating routine.
  *
  * - n must equal nx*ny*n_state and be at most 2,097,152 (16 MiB of
  *   doubles); larger states are rejected with MKG_ERR_ARG.

@@ -1614,11 +1614,11 @@ int64_t mkg_schedule_preview(const double *events, int64_t n_events,
 /* ------------------------------------------------------------------------ */
 /*
  * mkg_set_state stages the caller's doubles in a device buffer that the
- * handle allocates with cudaMalloc on first use. Some callers cannot allow
- * that call at that moment: code that uploads a new state inside a region
- * being captured into a CUDA graph (cudaMalloc is not stream-ordered and
- * breaks the capture), or a host loop driving pacing in real time, where
- * cudaMalloc's implicit device-wide synchronisation stalls every stream.
+ * handle allocates with cudaMalloc on first use. Some callers must not make
+ * that call when they upload a state: a host loop driving pacing in real
+ * time, where cudaMalloc's implicit device-wide synchronisation stalls
+ * every stream, or a host that keeps device memory in its own pool or under
+ * a fixed budget, where a cudaMalloc outside that pool can fail.
  * mkg_set_state_static stages through the fixed array below instead.
  *
  * The array lives in the library's device image: every GPU on which the

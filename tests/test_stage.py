@@ -290,16 +290,21 @@ def test_neighbour_sync_equals_grid_barrier(decker, stage, shape):
 
 
 @pytest.mark.gpu
-def test_neighbour_sync_nan_halt():
+@pytest.mark.parametrize('shape', [(64, 40), (64, 400), (32, 900)])
+def test_neighbour_sync_nan_halt(shape):
     # A NaN halt stops every warp after the halting step, with neighbour
-    # synchronisation as with the grid barrier
+    # synchronisation as with the grid barrier. On tall grids most warps
+    # are many halo rows away from the warp that records the halt (the
+    # owner of cell 0); they must still leave after the halting step: no
+    # timeout, and the same final state.
     import test_oracle as to
     msgs = []
+    states = []
     for sync in ('barrier', 'neighbors'):
         p = myokit.Protocol()
         p.schedule(start=0, level=-80, duration=1.234)
         p.schedule(start=1.234, level=-47.13, duration=1000)
-        s = mg.SimulationCUDA(to._nan_model(), p, ncells=(64, 40), block=64,
+        s = mg.SimulationCUDA(to._nan_model(), p, ncells=shape, block=64,
                               min_blocks=1)
         s.set_paced_cell_list([[1, 1]])
         s._sync = sync
@@ -308,5 +313,9 @@ def test_neighbour_sync_nan_halt():
             s.run(5)
         assert s._last_kernel.sync == sync
         msgs.append(str(e.value))
+        s.reset()
+        s.run(5, report_nan=False)
+        states.append(s.state_array())
     assert 'Time:  1.23' in msgs[0]
     assert msgs[0] == msgs[1]
+    assert np.array_equal(states[0], states[1], equal_nan=True)

@@ -1,12 +1,13 @@
 """
 The allocation-free state upload, ``mkg_set_state_static``.
 
-Callers that cannot call cudaMalloc where they upload a state (inside a
-CUDA-graph stream capture, or in a real-time loop that cannot afford
-cudaMalloc's device-wide synchronisation) use this entry point instead of
-``mkg_set_state``. It stages through a fixed 16 MiB device array, so it
-must give exactly what ``mkg_set_state`` gives, call after call, and must
-refuse states larger than that array.
+Callers that must not call cudaMalloc where they upload a state (a
+real-time pacing loop that cannot afford cudaMalloc's device-wide
+synchronisation, or a host that keeps device memory in its own pool or
+under a fixed budget) use this entry point instead of ``mkg_set_state``.
+It stages through a fixed 16 MiB device array, so it must give exactly
+what ``mkg_set_state`` gives, call after call, and must refuse states
+larger than that array.
 
 This file is named so that pytest collects it last.
 """
@@ -91,3 +92,42 @@ def test_static_upload_rejects_oversized_state():
         be.check(be.lib.mkg_set_state_static(be.h, _lib.dptr(state), n))
     with pytest.raises(_lib.MkgError, match='must have size'):
         be.check(be.lib.mkg_set_state_static(be.h, _lib.dptr(state), n - 1))
+
+
+def test_static_upload_allocates_nothing(br77):
+    # On a handle that never staged a state through mkg_set_state (so the
+    # handle's own staging buffer does not exist), the static upload takes
+    # no device memory: free device memory is unchanged, while the
+    # allocating upload of the same 16 MB state then takes some.
+    import torch
+    s0, be0 = _handle(br77, 40, myokit.DOUBLE_PRECISION)
+    st0 = np.ascontiguousarray(s0.state_array())
+    # Loads the library's device image and looks up the array's address
+    be0.check(be0.lib.mkg_set_state_static(be0.h, _lib.dptr(st0), st0.size))
+    s = mg.SimulationCUDA(br77, ncells=250000,
+                          precision=myokit.DOUBLE_PRECISION)
+    be = s._get_backend(s._kernel([]))   # a new handle, no state uploaded
+    state = np.ascontiguousarray(s.state_array())
+    n = state.size                       # 2,000,000 values, 16 MB
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    be.check(be.lib.mkg_set_state_static(be.h, _lib.dptr(state), n))
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0
+    got = _download(be, n)
+    assert np.array_equal(got, state)
+    be.check(be.lib.mkg_set_state(be.h, _lib.dptr(state), n))
+    free2 = torch.cuda.mem_get_info()[0]
+    assert free2 < free1
+
+
+def test_static_upload_refuses_accumulated_states(br77):
+    # FP32 kernels with FP64 or compensated V and concentrations keep extra
+    # planes that only mkg_set_state fills
+    s = mg.SimulationCUDA(br77, ncells=30, accumulate='kahan')
+    s.run(0.01)
+    be = s._backend[1]
+    state = np.ascontiguousarray(s.state_array())
+    with pytest.raises(_lib.MkgError, match='use mkg_set_state'):
+        be.check(be.lib.mkg_set_state_static(be.h, _lib.dptr(state),
+                                             state.size))
