@@ -2,26 +2,33 @@
 """
 Headline benchmark: cell-steps/s of the fused tissue step on one GB300.
 
-Workload (a 2D sheet as in the reference's SimulationOpenCL use):
-  512 x 512 cells, Rush-Larsen on, dt = 0.005 ms, the 4 left columns paced
-  by a 1 Hz protocol (2 ms pulses, level 1), per-cell GKr and GNa scale
-  fields lognormal(0, 0.2) from a seed, V logged every 1 ms at 256 seeded
-  random probe cells. The O'Hara-Rudy 2011 model file is not available, so
-  the 48-state Decker 2009 canine model shipped with myokit stands in.
+Headline workload (the large-sheet configuration):
+  a 2048 x 2048 sheet of the 48-state Decker 2009 canine model (standing in
+  for O'Hara-Rudy 2011 endo, whose model file is not available), Rush-Larsen
+  on, dt = 0.005 ms, single precision with Kahan-compensated V and
+  concentrations; S1 on the 4 left columns at t = 0 (2 ms, level 1), S2 on
+  the lower-left quadrant at t = 320 ms; the full V frame every 5 ms
+  recorded in a device buffer.
 
-One bench step = ``run(step_ms)`` of that sheet (2000 time steps at the
-default 10 ms). ``value`` is cell-steps per second of device time with the
-state resident in HBM (CUDA events on the simulation's stream around the
-kernel launches); ``e2e`` is the same metric through the public
-``SimulationCUDA.run`` call, state upload, log and final state download
-included. Single precision is the headline; double precision is timed on
-the same sheet and the largest |dV| between the two at the probes is
-reported.
+One bench step = ``run_frames(step_ms, 5)`` of that sheet (2000 time steps
+at the default 10 ms). ``value`` is cell-steps per second of device time
+with the state resident in HBM (CUDA events on the library's stream around
+the kernel launches); ``e2e`` is the same metric through the public call,
+with the host state uploaded, and the frames and the final state read back
+to the host, every step. The state (805 MB, plus 134 MB of compensation
+planes) is far larger than L2, so no flush is needed between steps.
+
+Also reported: the plain FP64 path on the same sheet; max|dV|, activation
+and APD90 errors of the headline precision against FP64 at full size (the
+S1 phase, and a window after S2); the 512 x 512 sheet (the medium
+configuration, L2-resident, bound by instruction issue) in every precision
+mode; the adjoint; the 200-cell FP64 cable; the 512 batched cables; and the
+reference's CPU rate on the host cores.
 
 --impl reference times the reference's own kernel (the OpenCL C that
-myokit's SimulationOpenCL renders for this model, compiled for the host
-CPU and driven by the oracle's restatement of the reference step loop) on
-all host cores, with the same metric and configuration.
+myokit's SimulationOpenCL renders for this model, compiled for the host CPU
+and driven through the reference's unmodified Python layer by the oracle's
+restatement of its step loop) on all host cores, on the same configuration.
 """
 import argparse
 import json
@@ -37,15 +44,17 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = 'cell-steps/s on 1 GB300 (FP32 vs FP64 at stated max|dV|)'
+UNIT = 'cell-steps/s'
+FRAME_MS = 5.0      # the headline sheet's frame interval
+S2_AT = 320.0       # S2 time of the headline protocol
 
-# Single precision variants: FP64 or compensated accumulation of V and the
-# concentrations, and the fast FP32 arithmetic option
+# Single precision variants of the 512 x 512 sheet: FP64 or compensated
+# accumulation of V and the concentrations, and IEEE division
 VARIANTS = [
     ('fp32+double', {'accumulate': 'double'}),
     ('fp32+kahan', {'accumulate': 'kahan'}),
     ('fp32-ieee-div', {'fp32_math': 'ieee'}),
 ]
-UNIT = 'cell-steps/s'
 
 
 def parse():
@@ -54,29 +63,40 @@ def parse():
     p.add_argument('--steps', type=int, default=10)
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    p.add_argument('--size', type=int, default=512)
-    p.add_argument('--step-ms', type=float, default=10.0)
+    p.add_argument('--size', type=int, default=2048,
+                   help='edge of the headline sheet')
+    p.add_argument('--step-ms', type=float, default=10.0,
+                   help='simulated time per bench step')
+    p.add_argument('--fp64-ms', type=float, default=1.0,
+                   help='simulated time of the timed FP64 run of the'
+                        ' headline sheet (0 = skip)')
+    p.add_argument('--s1-ms', type=float, default=S2_AT,
+                   help='window of the full-size precision comparison before'
+                        ' S2 (0 = skip the comparison)')
+    p.add_argument('--s2-ms', type=float, default=10.0,
+                   help='window of the full-size precision comparison after'
+                        ' S2 (FP64 on the whole sheet; 0 = skip)')
+    p.add_argument('--sheet512-steps', type=int, default=5,
+                   help='timed steps of the 512 x 512 sheet (0 = skip it)')
     p.add_argument('--fp64-steps', type=int, default=2,
-                   help='timed double precision bench steps (0 = skip)')
+                   help='timed double precision steps of the 512 x 512'
+                        ' sheet (0 = skip)')
     p.add_argument('--variant-steps', type=int, default=3,
-                   help='timed steps of the FP64/Kahan accumulation variants')
+                   help='timed steps of the 512 x 512 accumulation variants')
     p.add_argument('--accuracy-ms', type=float, default=400.0,
-                   help='simulated time of the precision comparison runs'
-                        ' (0 = skip)')
+                   help='simulated time of the 128 x 128 and 24 x 24'
+                        ' precision comparisons (0 = skip)')
     p.add_argument('--adjoint-ms', type=float, default=300.0,
                    help='simulated time of the adjoint measurement (the'
                         ' 256 x 256 adjoint configuration runs 300 ms;'
                         ' 0 = skip)')
-    p.add_argument('--configs', default='c1,c3,c5',
+    p.add_argument('--configs', default='c1,c3',
                    help='other configurations to time: comma list of c1'
-                        ' (200-cell FP64 cable), c3 (512 batched cables), c5'
-                        ' (2048x2048 S1-S2 sheet), or none')
-    p.add_argument('--c5-full', action='store_true',
-                   help='run the whole 1000 ms S1-S2 protocol of the'
-                        ' 2048x2048 sheet instead of a 20 ms window')
+                        ' (200-cell FP64 cable), c3 (512 batched cables), or'
+                        ' none')
     p.add_argument('--full', action='store_true',
-                   help='run every configuration at its full length: the'
-                        ' batched cables for 2000 ms, the adjoint over'
+                   help='also run every configuration at its full length:'
+                        ' the batched cables for 2000 ms, the adjoint over'
                         ' 300 ms, the 2048x2048 S1-S2 protocol for 1000 ms')
     p.add_argument('--profile', action='store_true',
                    help='run one small sheet case for a profiler and exit')
@@ -110,7 +130,9 @@ def parse():
                    help='also write the raw nvidia-smi clock samples of the'
                         ' timed region to this CSV file')
     p.add_argument('--cpu-seconds', type=float, default=12.0,
-                   help='target CPU work for the cpu_baseline sample')
+                   help='target CPU time of the cpu_baseline sample')
+    p.add_argument('--ref-seconds', type=float, default=5.0,
+                   help='target CPU time of one --impl reference step')
     return p.parse_args()
 
 
@@ -122,7 +144,8 @@ def load_model():
 
 
 def make_sheet(cls, precision, size, seed=0, fields=True, **kw):
-    """The benchmark sheet; returns (simulation, log variable list)."""
+    """The 512 x 512 benchmark sheet (medium configuration, any size);
+    returns (simulation, log variable list)."""
     from myokit_gb300._deps import myokit
     m = load_model()
     p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
@@ -141,17 +164,59 @@ def make_sheet(cls, precision, size, seed=0, fields=True, **kw):
     return s, log
 
 
-def config(args, workload):
+def make_s1_sheet(cls, precision, n, **kw):
+    """The headline sheet before S2: n x n, no fields, S1 on the 4 left
+    columns at t = 0 (a 1 Hz block train of 2 ms pulses, level 1)."""
+    from myokit_gb300._deps import myokit
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    s = cls(load_model(), p, ncells=(n, n), precision=precision, rl=True,
+            **kw)
+    s.set_step_size(0.005)
+    s.set_paced_cells(nx=4, ny=n, x=0, y=0)
+    return s
+
+
+def make_s1_cable(cls, precision, n, **kw):
+    """One row of the S1 sheet as a 1D cable (gx = 10, the sheet's default;
+    the first 4 cells paced). Every row of the S1 sheet equals it."""
+    from myokit_gb300._deps import myokit
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    s = cls(load_model(), p, ncells=n, precision=precision, rl=True, **kw)
+    s.set_step_size(0.005)
+    s.set_conductance(10)
+    s.set_paced_cells(4)
+    return s
+
+
+def apply_s2(s, n):
+    """Switches a sheet at t = 320 ms to the S2 stimulus: the lower-left
+    quadrant paced once, at 320 ms (2 ms, level 1)."""
+    from myokit_gb300._deps import myokit
+    s.set_paced_cells(nx=n // 2, ny=n // 2, x=0, y=0)
+    p2 = myokit.Protocol()
+    p2.schedule(level=1, start=S2_AT, duration=2)
+    s.set_protocol(p2)
+
+
+def config(args):
+    """The headline configuration (identical for both arms)."""
+    n = args.size
     return {
-        'workload': workload,
+        'workload': 'sheet %dx%d, S1-S2 protocol, full V frame every 5 ms'
+                    ' to a device buffer, %d time steps per step' % (
+                        n, n, int(round(args.step_ms / 0.005))),
         'model': 'decker-2009 (48 states; stands in for O\'Hara-Rudy 2011'
                  ' endo, whose model file is unavailable)',
-        'grid': [args.size, args.size],
-        'rl': True, 'dt_ms': 0.005, 'step_ms': args.step_ms,
-        'paced': 'left 4 columns, 1 Hz, 2 ms, level 1',
-        'fields': 'GKr, GNa x lognormal(0, 0.2), seed 0',
-        'log': 'V at 256 probes every 1 ms',
-        'l2': 'flushed between timed steps (256 MiB write)',
+        'grid': [n, n], 'rl': True, 'dt_ms': 0.005,
+        'step_ms': args.step_ms,
+        'paced': 'left 4 columns, S1 at 0 ms (2 ms, level 1); lower-left'
+                 ' quadrant, S2 at 320 ms',
+        'fields': 'none',
+        'log': 'full V frame every 5 ms (device buffer)',
+        'l2': ('inputs larger than L2 (state %.0f MB), no flush' if
+               n * n * 48 * 4 > 129e6 else
+               'state of %.1f MB, smaller than L2, not flushed') % (
+                   n * n * 48 * 4 / 1e6),
     }
 
 
@@ -228,44 +293,384 @@ def read_peaks():
         return 6800.0, 'fallback'
 
 
-def read_traffic():
-    """Per-cell-step DRAM bytes of the tissue kernel from the committed ncu
-    summary, or None."""
+def read_traffic(workload):
+    """Per-cell-step DRAM bytes and warp instructions of the tissue kernel
+    on one workload, from the committed ncu summaries, or None."""
     path = os.path.join(ROOT, 'profiles', 'tissue_step_traffic.json')
     try:
         with open(path) as f:
-            return json.load(f)
+            return json.load(f).get(workload)
     except (OSError, ValueError):
         return None
 
 
-def cpu_baseline(args, precision, seconds):
-    """Times the reference kernel on the host cores for a bounded sample."""
+def sm_count(device):
+    import torch
+    return torch.cuda.get_device_properties(device).multi_processor_count
+
+
+def issue_roofline(traffic, value, sm_mhz, n_sm):
+    """Instruction-issue roofline: warp instructions per cell-step (from an
+    ncu capture) against 4 schedulers per SM issuing one per clock."""
+    if not traffic or not traffic.get('warp_instructions_per_cell_step'):
+        return None
+    ach = traffic['warp_instructions_per_cell_step'] * value
+    peak = 4 * n_sm * sm_mhz * 1e6
+    return {'unit': 'warp instructions/s', 'achieved': ach, 'peak': peak,
+            'frac': ach / peak,
+            'warp_instructions_per_cell_step':
+                traffic['warp_instructions_per_cell_step'],
+            'source': traffic.get('source')}
+
+
+class _ChunkClock(object):
+    """
+    Progress reporter for the reference's run(): the reference calls
+    update() after every sim_step, so the times between calls are the
+    times of its step-loop chunks. After a calibration chunk it sets the
+    chunk length for about ``seconds`` of CPU time, and it cancels the run
+    after ``n_warm + n_timed`` further chunks.
+    """
+    def __init__(self, backend, ncell, seconds, n_warm, n_timed):
+        self.be = backend
+        self.ncell = ncell
+        self.seconds = seconds
+        self.n_warm = n_warm
+        self.n_timed = n_timed
+        self.marks = []
+        self.steps = None
+
+    def enter(self, msg=None):
+        self.marks = [time.perf_counter()]
+
+    def exit(self):
+        pass
+
+    def update(self, progress):
+        self.marks.append(time.perf_counter())
+        if len(self.marks) == 2:
+            dt = self.marks[1] - self.marks[0]
+            rate = self.ncell * self.be.chunk_steps / max(dt, 1e-9)
+            self.steps = int(max(1, min(20000, round(
+                rate * self.seconds / self.ncell))))
+            self.be.chunk_steps = self.steps
+            return True
+        return len(self.marks) < 2 + self.n_warm + self.n_timed
+
+
+def reference_rate(n, precision, seconds, n_warm, n_timed, cores=None):
+    """
+    Times the reference's kernel on the host cores on the headline sheet
+    through the reference's own run() (myokit.SimulationOpenCL with the
+    oracle's CPU backend). The chunks of its step loop are timed after its
+    per-run set-up (kernel rendering, Python-list marshalling of the state),
+    which is left out, to the reference's advantage. Returns (cell-steps/s,
+    time steps per chunk, chunk seconds, threads).
+    """
+    from myokit_gb300._deps import myokit
     from oracle.refsim import ReferenceCpuSimulation
-    cores = os.cpu_count() or 1
-    s, _ = make_sheet(ReferenceCpuSimulation, precision, args.size)
+    cores = cores or os.cpu_count() or 1
+    s = make_s1_sheet(ReferenceCpuSimulation, precision, n)
     s.set_threads(cores)
-    ncell = args.size * args.size
-    # Calibrate on a short run, then size the sample
-    t0 = time.perf_counter()
-    s.run(0.05, log=['engine.time'], log_interval=1)   # 10 steps
-    dt = time.perf_counter() - t0
-    rate0 = ncell * 10 / max(dt, 1e-9)
-    nsteps = int(max(20, min(20000, rate0 * seconds / ncell)))
-    t0 = time.perf_counter()
-    s.run(nsteps * 0.005, log=['engine.time'], log_interval=1)
-    dt = time.perf_counter() - t0
+    be = s._sim
+    be.chunk_steps = 2          # the calibration chunk
+
+    class Clock(_ChunkClock, myokit.ProgressReporter):
+        pass
+    clock = Clock(be, n * n, seconds, n_warm, n_timed)
+    try:
+        s.run(1000, log=['engine.time'], log_interval=FRAME_MS,
+              progress=clock)
+    except myokit.SimulationCancelledError:
+        pass
+    be.chunk_steps = None
+    times = np.diff(clock.marks)[1 + n_warm:1 + n_warm + n_timed]
+    rate = n * n * clock.steps * len(times) / float(np.sum(times))
+    return rate, clock.steps, [float(x) for x in times], cores
+
+
+def cpu_baseline(args):
+    """The reference's CPU rate on a bounded sample of the headline sheet."""
+    from myokit_gb300._deps import myokit
+    rate, steps, times, cores = reference_rate(
+        args.size, myokit.SINGLE_PRECISION, args.cpu_seconds, 0, 1)
     return {
-        'value': ncell * nsteps / dt, 'unit': UNIT, 'cores': cores,
-        'kind': 'reference',
-        'sample': '%d time steps (%.3g ms) of the %dx%d sheet, %s; the'
-                  ' reference-rendered OpenCL kernel compiled as C (gcc -O2,'
-                  ' OpenMP) with the oracle host loop' % (
-                      nsteps, nsteps * 0.005, args.size, args.size,
-                      'single precision' if precision == 32 else
-                      'double precision'),
-        'seconds': dt,
+        'value': rate, 'unit': UNIT, 'cores': cores, 'kind': 'reference',
+        'sample': '%d time steps (%.3g ms) of the %dx%d sheet in single'
+                  ' precision (the reference has no compensated mode),'
+                  ' timed inside one run() of the reference after its'
+                  ' per-run set-up; the reference-rendered OpenCL kernel'
+                  ' compiled as C (gcc -O2, OpenMP, %d threads) with the'
+                  ' oracle host loop' % (steps, steps * 0.005, args.size,
+                                         args.size, cores),
+        'seconds': sum(times),
     }
+
+
+def run_reference(args):
+    """--impl reference: the reference kernel on the host cores."""
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return 0
+    from myokit_gb300._deps import myokit
+    rate, steps, times, cores = reference_rate(
+        args.size, myokit.SINGLE_PRECISION, args.ref_seconds, args.warmup,
+        args.steps)
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': rate, 'unit': UNIT,
+        'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': 1000 * float(np.mean(times)),
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32', 'data': 'synthetic (seeded probes)',
+        'precision': 'FP32 (the reference has no compensated mode)',
+        'config': config(args),
+        'cpu_baseline': {
+            'value': rate, 'unit': UNIT, 'cores': cores,
+            'kind': 'reference',
+            'sample': 'each step: %d time steps (%.3g ms) of the %dx%d'
+                      ' sheet, one chunk of the reference step loop inside'
+                      ' one run() of the reference (its per-run kernel'
+                      ' rendering and state marshalling are outside the'
+                      ' timed chunks; no frames are logged)' % (
+                          steps, steps * 0.005, args.size, args.size)},
+        'e2e': {'value': rate, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def c5_accuracy(args, device):
+    """
+    Max |dV|, activation-time and APD90 errors of the headline precision
+    (FP32 + Kahan) against FP64, on the full 2048 x 2048 sheet.
+
+    - S1 phase (0 to 320 ms): the sheet paced along its whole left edge has
+      identical rows, so its FP64 solution is a 2048-cell FP64 cable (the
+      FP64 sheet's rows equal the cable bit for bit; checked by the fp64
+      block). 256 probe traces every 0.1 ms against the cable's traces at
+      their x, and the whole V plane at 320 ms against the cable's V.
+    - After S2 (320 ms on): the FP64 sheet itself, started from the FP64
+      cable state broadcast to every row, against the FP32 + Kahan sheet
+      continuing from its own state; probe traces and the whole V plane at
+      the end of the window.
+    """
+    import torch
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+    from myokit_gb300 import metrics
+    SP, DP = myokit.SINGLE_PRECISION, myokit.DOUBLE_PRECISION
+    n = args.size
+    rng = np.random.default_rng(7)
+    cells = sorted(rng.choice(n * n, 256, replace=False))
+    xy = [(int(c % n), int(c // n)) for c in cells]
+    keys = ['%d.%d.membrane.V' % p for p in xy]
+    log = ['engine.time'] + keys
+    out = {}
+
+    # S1 phase
+    t1 = args.s1_ms
+    s32 = make_s1_sheet(mg.SimulationCUDA, SP, n, accumulate='kahan',
+                        device=device)
+    d32 = s32.run(t1, log=log, log_interval=0.1)
+    c64 = make_s1_cable(mg.SimulationCUDA, DP, n, device=device)
+    xs = sorted(set(x for x, _ in xy))
+    dc = c64.run(t1, log=['engine.time'] + ['%d.membrane.V' % x
+                                            for x in xs], log_interval=0.1)
+    t = np.asarray(dc['engine.time'])
+    # the single precision log holds the float32 rounding of the times
+    assert np.array_equal(np.asarray(d32['engine.time']),
+                          t.astype(np.float32))
+    got = {k: np.asarray(d32[k]) for k in keys}
+    ref = {k: np.asarray(dc['%d.membrane.V' % x]) for k, (x, _) in
+           zip(keys, xy)}
+    res = metrics.compare(t, got, ref)
+    i_vm = s32._vm.index()
+    ns = s32._nstate
+    v32 = s32.state_array().reshape(n, n, ns)[:, :, i_vm]
+    st64 = c64.state_array().reshape(n, ns)
+    res['full_sheet_max_abs_dV_mV_at_end'] = float(
+        np.max(np.abs(v32 - st64[None, :, i_vm])))
+    res['activated_traces'] = int(sum(
+        np.isfinite(metrics.activation_time(t, ref[k])) for k in keys))
+    out['s1_phase'] = dict(
+        res, window_ms=[0.0, t1], probes=len(keys), log_interval_ms=0.1,
+        reference='FP64 %d-cell cable on the GPU (every row of the S1'
+                  ' sheet equals it)' % n)
+    del v32
+
+    # After S2
+    if args.s2_ms > 0 and abs(t1 - S2_AT) < 1e-9:
+        s64 = make_s1_sheet(mg.SimulationCUDA, DP, n, device=device)
+        s64.set_state(np.tile(st64.reshape(-1), n))
+        s64.set_time(t1)
+        for s in (s32, s64):
+            apply_s2(s, n)
+        d32 = s32.run(args.s2_ms, log=log, log_interval=0.1)
+        d64 = s64.run(args.s2_ms, log=log, log_interval=0.1)
+        t = np.asarray(d64['engine.time'])
+        res = metrics.compare(t, {k: np.asarray(d32[k]) for k in keys},
+                              {k: np.asarray(d64[k]) for k in keys})
+        v32 = s32.state_array().reshape(n, n, ns)[:, :, i_vm]
+        v64 = s64.state_array().reshape(n, n, ns)[:, :, i_vm]
+        res['full_sheet_max_abs_dV_mV_at_end'] = float(
+            np.max(np.abs(v32 - v64)))
+        res['s2_activated_fraction_at_end'] = float(np.mean(
+            (v64[:n // 2, :n // 2] > -40)))
+        out['after_s2'] = dict(
+            res, window_ms=[t1, t1 + args.s2_ms], probes=len(keys),
+            log_interval_ms=0.1,
+            reference='FP64 %dx%d sheet on the GPU, started from the FP64'
+                      ' cable state at %g ms' % (n, n, t1))
+        del s64, v64, v32
+    del s32, c64
+    torch.cuda.empty_cache()
+    return out
+
+
+def c5_fp64(args, device, value):
+    """
+    The plain FP64 path on the headline sheet, timed over args.fp64_ms;
+    its rows are checked against the FP64 cable bit for bit.
+    """
+    import torch
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+    DP = myokit.DOUBLE_PRECISION
+    n = args.size
+    s64 = make_s1_sheet(mg.SimulationCUDA, DP, n, device=device)
+    s64.run(0.05, log=['engine.time'], log_interval=1)
+    s64.run(args.fp64_ms, log=['engine.time'], log_interval=1)
+    st = s64.last_run_stats()
+    v64 = st['cell_steps'] / (st['kernel_ms'] / 1000)
+    x = s64.state_array().reshape(n, n, -1)
+    del s64
+    c = make_s1_cable(mg.SimulationCUDA, DP, n, device=device)
+    c.run(0.05, log=['engine.time'], log_interval=1)
+    c.run(args.fp64_ms, log=['engine.time'], log_interval=1)
+    rows = bool(np.array_equal(x, np.broadcast_to(
+        c.state_array().reshape(1, n, -1), x.shape)))
+    del x
+    torch.cuda.empty_cache()
+    return {'value': v64, 'unit': UNIT, 'window_ms': args.fp64_ms,
+            'speedup_fp32_kahan_over_fp64': value / v64,
+            'rows_equal_fp64_cable': rows}
+
+
+def c5_full(args, device):
+    """The whole 1000 ms S1-S2 protocol of the headline sheet (--full)."""
+    import torch
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+    n = args.size
+    s = make_s1_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION, n,
+                      accumulate='kahan', device=device)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, f1 = s.run_frames(S2_AT, FRAME_MS)
+    ms = s.last_run_stats()['kernel_ms']
+    apply_s2(s, n)
+    _, f2 = s.run_frames(1000 - S2_AT, FRAME_MS)
+    ms += s.last_run_stats()['kernel_ms']
+    wall = time.perf_counter() - t0
+    frames = torch.cat([f1, f2])
+    steps = 200000
+    out = {'window_ms': 1000, 'frames': int(frames.shape[0]),
+           'frame_bytes': int(frames[0].numel() * frames.element_size()),
+           'value': n * n * steps / (ms / 1000),
+           'e2e_frames_on_device': n * n * steps / wall, 'unit': UNIT,
+           'final_v_range_mV': [float(frames[-1].min()),
+                                float(frames[-1].max())],
+           'activated_fraction_final': float(
+               (frames[-1] > -40).float().mean())}
+    del s, frames, f1, f2
+    torch.cuda.empty_cache()
+    return out
+
+
+def sheet512_runs(args, device, n_sm):
+    """
+    The 512 x 512 sheet (medium configuration: GKr/GNa lognormal fields,
+    V at 256 probes every 1 ms): FP32 device and end-to-end rates with L2
+    flushed between steps, its instruction-issue roofline (the state is
+    L2-resident, so issue binds), FP64 on the same sheet, and the FP32
+    accumulation and division variants.
+    """
+    import torch
+    from myokit_gb300._deps import myokit
+    import myokit_gb300 as mg
+    SP, DP = myokit.SINGLE_PRECISION, myokit.DOUBLE_PRECISION
+    size = 512
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    out = {'grid': [size, size], 'step_ms': args.step_ms,
+           'fields': 'GKr, GNa x lognormal(0, 0.2), seed 0',
+           'log': 'V at 256 probes every 1 ms',
+           'l2': 'flushed between timed steps (256 MiB write)'}
+
+    def timed(s, log, steps, warm):
+        dms, wall, ncs, logs = 0.0, 0.0, 0, []
+        for i in range(warm + steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            logs.append(s.run(args.step_ms, log=log, log_interval=1))
+            if i >= warm:
+                wall += time.perf_counter() - t0
+                st = s.last_run_stats()
+                dms += st['kernel_ms']
+                ncs += st['cell_steps']
+        return ncs / (dms / 1000), ncs / wall, logs
+
+    s, log = make_sheet(mg.SimulationCUDA, SP, size, device=device)
+    value, e2e, logs32 = timed(s, log, args.sheet512_steps, 3)
+    k = s._last_kernel
+    peak, kind = read_peaks()
+    bpcs = k.bytes_per_cell_step()
+    traffic = read_traffic('sheet512_fp32')
+    out.update({'precision': 'fp32', 'fp32_math': s._fp32_math,
+                'value': value, 'e2e': e2e, 'unit': UNIT})
+    out['roofline'] = {
+        'bound': 'issue',
+        'issue': None, 'hbm_equivalent': {
+            'bytes_per_cell_step': bpcs, 'achieved': value * bpcs / 1e9,
+            'peak': peak, 'unit': 'GB/s', 'peak_source': kind,
+            'frac': value * bpcs / 1e9 / peak,
+            'dram_bytes_per_cell_step':
+                traffic and traffic.get('bytes_per_cell_step')}}
+    out['_issue_inputs'] = (traffic, value)
+    del s
+    if args.fp64_steps > 0:
+        s64, _ = make_sheet(mg.SimulationCUDA, DP, size, device=device)
+        v64, _, logs64 = timed(s64, log, args.fp64_steps, 3)
+        worst = 0.0
+        for a, b in zip(logs32, logs64):
+            for key in a.keys():
+                if key == 'engine.time':
+                    continue
+                worst = max(worst, float(np.max(np.abs(
+                    np.asarray(a[key], dtype=float) -
+                    np.asarray(b[key], dtype=float)))))
+        out['fp64'] = {'value': v64, 'unit': UNIT,
+                       'speedup_fp32_over_fp64': value / v64,
+                       'max_abs_dV_fp32_vs_fp64_mV': worst,
+                       'dV_window_ms': len(logs64) * args.step_ms}
+        del s64
+    variants = {}
+    if args.variant_steps > 0:
+        for vname, kw in VARIANTS:
+            sv, _ = make_sheet(mg.SimulationCUDA, SP, size, device=device,
+                               **kw)
+            v, _, _ = timed(sv, log, args.variant_steps, 3)
+            variants[vname] = {
+                'value': v, 'unit': UNIT,
+                'accumulated_states': [x.qname()
+                                       for x in sv.accumulated_states()],
+                'bytes_per_cell_step': sv._last_kernel.bytes_per_cell_step()}
+            del sv
+    out['variants'] = variants
+    del flush
+    torch.cuda.empty_cache()
+    return out
 
 
 def accuracy_runs(args, device):
@@ -426,7 +831,28 @@ def adjoint_runs(args, device):
                         'fd': fd, 'rel_err': rel})
     out['fd_check_sheet64_fp64'] = {
         'window_ms': fd_ms, 'entries': len(entries),
-        'max_rel_err': worst, 'loss': L, 'sample': entries[:4]}
+        'max_rel_err': worst, 'loss': L, 'sample': entries[:4],
+        'precision': 'fp64 forward and adjoint (the precision that meets'
+                     ' the 1e-4 bar)'}
+
+    # The adjoint configuration's precision (FP32 with FP64 V and
+    # concentrations) against the same FP64 finite differences
+    s, _ = make_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION, n,
+                      seed=0, device=device, accumulate='double')
+    adj = ad.TissueAdjoint(s, probes, segment_steps=200)
+    L32, g32 = adj.loss_and_gradient(fd_ms, target, 1.0)
+    errs = []
+    for e in entries:
+        ix, iy = e['cell']
+        a = g32[e['field']][iy, ix]
+        errs.append(abs(a - e['fd']) / max(abs(e['fd']), 1e-12 * abs(L)))
+    out['fd_check_sheet64_fp32_double'] = {
+        'window_ms': fd_ms, 'entries': len(errs),
+        'max_rel_err': float(max(errs)),
+        'median_rel_err': float(np.median(errs)), 'loss': L32,
+        'precision': 'fp32 forward and adjoint with FP64 V and'
+                     ' concentrations, against central differences of the'
+                     ' FP64 forward'}
     return out
 
 
@@ -542,82 +968,6 @@ def _cables(m, p, **kw):
     return batch.sim, batch
 
 
-def config_c5(args, device):
-    """
-    Large: a 2048 x 2048 sheet, single precision with Kahan-compensated V
-    and concentrations, dt 0.005 ms; S1 on the left edge at t = 0, then S2
-    on the lower-left quadrant at t = 320 ms; the full V frame every 5 ms
-    recorded in a device buffer (run_frames). Timed over a 20 ms window,
-    or the whole 1000 ms with --c5-full.
-    """
-    import torch
-    from myokit_gb300._deps import myokit
-    import myokit_gb300 as mg
-    n = 2048
-    m = load_model()
-    s1 = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
-    s = mg.SimulationCUDA(m, s1, ncells=(n, n), rl=True, accumulate='kahan',
-                          device=device)
-    s.set_step_size(0.005)
-    s.set_paced_cells(nx=4, ny=n, x=0, y=0)
-    s.run_frames(1, 5)
-    s.reset()
-    out = {'grid': [n, n]}
-    torch.cuda.synchronize()
-    if args.c5_full or args.full:
-        t0 = time.perf_counter()
-        t1_, f1 = s.run_frames(320, 5)
-        ms = s.last_run_stats()['kernel_ms']
-        s.set_paced_cells(nx=n // 2, ny=n // 2, x=0, y=0)
-        p2 = myokit.Protocol()
-        p2.schedule(level=1, start=320, duration=2)
-        s.set_protocol(p2)
-        t2_, f2 = s.run_frames(680, 5)
-        ms += s.last_run_stats()['kernel_ms']
-        wall = time.perf_counter() - t0
-        frames = torch.cat([f1, f2])
-        steps = 200000
-        out.update({'window_ms': 1000, 'frames': int(frames.shape[0]),
-                    'frame_bytes': int(frames[0].numel() *
-                                       frames.element_size()),
-                    'final_v_range_mV': [float(frames[-1].min()),
-                                         float(frames[-1].max())],
-                    'activated_fraction_final': float(
-                        (frames[-1] > -40).float().mean())})
-    else:
-        t0 = time.perf_counter()
-        tt, frames = s.run_frames(20, 5)
-        wall = time.perf_counter() - t0
-        ms = s.last_run_stats()['kernel_ms']
-        steps = 4000
-        out.update({'window_ms': 20, 'frames': int(frames.shape[0])})
-    out['value'] = n * n * steps / (ms / 1000)
-    out['e2e'] = n * n * steps / wall
-    out['unit'] = UNIT
-    k = s._last_kernel
-    peak, kind = read_peaks()
-    bpcs = k.bytes_per_cell_step()
-    out['roofline'] = {'bound': 'hbm', 'bytes_per_cell_step': bpcs,
-                       'achieved': out['value'] * bpcs / 1e9, 'peak': peak,
-                       'unit': 'GB/s', 'peak_source': kind,
-                       'frac': out['value'] * bpcs / 1e9 / peak}
-    del s, frames
-    torch.cuda.empty_cache()
-
-    # The plain FP64 path on the same sheet, over 1 ms (200 steps)
-    s64 = mg.SimulationCUDA(m, s1, ncells=(n, n), rl=True, device=device,
-                            precision=myokit.DOUBLE_PRECISION)
-    s64.set_step_size(0.005)
-    s64.set_paced_cells(nx=4, ny=n, x=0, y=0)
-    s64.run(0.05, log=['engine.time'], log_interval=1)
-    s64.run(1, log=['engine.time'], log_interval=1)
-    st = s64.last_run_stats()
-    v64 = st['cell_steps'] / (st['kernel_ms'] / 1000)
-    out['fp64'] = {'value': v64, 'unit': UNIT, 'window_ms': 1}
-    out['speedup_over_fp64'] = out['value'] / v64
-    return out
-
-
 def tune_configs(args):
     """
     Runs the autotuner on each benchmark configuration: the 512 x 512 sheet
@@ -731,51 +1081,14 @@ def profile_case(args):
     return 0
 
 
-def run_reference(args):
-    """--impl reference: the reference kernel on the host cores."""
-    rank = int(os.environ.get('RANK', '0'))
-    if rank != 0:
-        return 0
-    from myokit_gb300._deps import myokit
-    from oracle.refsim import ReferenceCpuSimulation
-    cores = os.cpu_count() or 1
-    s, log = make_sheet(ReferenceCpuSimulation, myokit.SINGLE_PRECISION,
-                        args.size)
-    s.set_threads(cores)
-    ncell = args.size * args.size
-    # Bench step: a bounded sample sized to ~2 s of CPU time (calibrated
-    # after a first run, which also builds the reference kernel)
-    s.run(0.05, log=log, log_interval=1)
-    t0 = time.perf_counter()
-    s.run(0.05, log=log, log_interval=1)
-    rate0 = ncell * 10 / max(time.perf_counter() - t0, 1e-9)
-    nsteps = int(max(10, min(2000, rate0 * 2.0 / ncell)))
-    dur = nsteps * 0.005
-    for _ in range(args.warmup):
-        s.run(dur, log=log, log_interval=1)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        s.run(dur, log=log, log_interval=1)
-    dt = time.perf_counter() - t0
-    value = ncell * nsteps * args.steps / dt
-    line = {
-        'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT,
-        'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': dt * 1000 / args.steps, 'higher_is_better': True,
-        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-        'data': 'synthetic (seeded fields and probes)',
-        'config': config(args, 'reference kernel on host CPU, %d time steps'
-                         ' per step' % nsteps),
-        'cpu_baseline': {
-            'value': value, 'unit': UNIT, 'cores': cores,
-            'kind': 'reference',
-            'sample': '%d time steps of the %dx%d sheet per step' % (
-                nsteps, args.size, args.size)},
-        'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0,
-                'd2h_bytes_per_step': 0},
-    }
-    print(json.dumps(line))
-    return 0
+def guarded(fn, *a):
+    """fn(*a), or {'error': ...} (traceback on stderr) if it raises."""
+    import traceback
+    try:
+        return fn(*a)
+    except Exception as e:
+        traceback.print_exc()
+        return {'error': '%s: %s' % (type(e).__name__, e)}
 
 
 def run_ours(args):
@@ -797,16 +1110,25 @@ def run_ours(args):
             dist.barrier(device_ids=[local])
         torch.cuda.synchronize()
 
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device='cuda')
-    ncell = args.size * args.size
+    n = args.size
+    ncell = n * n
+    n_sm = sm_count(local)
     nsteps_per = int(round(args.step_ms / 0.005))
 
-    # --- single precision (headline) -------------------------------------
-    s, log = make_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION,
-                        args.size, seed=rank, device=local)
-    logs32 = []
+    # --- headline: FP32 + Kahan sheet, frames on the device ---------------
+    s = make_s1_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION, n,
+                      accumulate='kahan', device=local)
+    s2_applied = [None]
+
+    def step():
+        # S2 switches on at the first step boundary at or after 320 ms
+        if s2_applied[0] is None and s.time() >= S2_AT - 1e-9:
+            apply_s2(s, n)
+            s2_applied[0] = s.time()
+        return s.run_frames(args.step_ms, FRAME_MS)
+
     for _ in range(args.warmup):
-        logs32.append(s.run(args.step_ms, log=log, log_interval=1))
+        step()
     kernel = s._last_kernel
     sampler = ClockSampler(args.clocks_csv)
     sampler.start()
@@ -816,19 +1138,26 @@ def run_ours(args):
     launches = 0
     step_launches = 0
     cell_steps = 0
+    frame_bytes = 0
+    n_frames = 0
     for _ in range(args.steps):
-        flush.fill_(1)
-        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        logs32.append(s.run(args.step_ms, log=log, log_interval=1))
+        tt, frames = step()
+        host = frames.cpu()         # the step's result, read back
         wall += time.perf_counter() - t0
         st = s.last_run_stats()
         dev_ms += st['kernel_ms']
         launches += st['all_launches']
         step_launches += st['launches']
         cell_steps += st['cell_steps']
+        frame_bytes += host.numel() * host.element_size() + 8 * len(tt)
+        n_frames += len(tt)
+        del host, frames
     barrier()
     clocks = sampler.stop()
+    t_end = s.time()
+    del s
+    torch.cuda.empty_cache()
     # Replicas: the slowest rank's times, every rank's cell-steps
     from myokit_gb300.replicas import combine
     dev_ms, wall, total_cell_steps = combine(
@@ -836,10 +1165,12 @@ def run_ours(args):
     value = total_cell_steps / (dev_ms / 1000.0)
     e2e_value = total_cell_steps / wall
 
-    # Bytes crossing the host boundary per bench step (public run() call)
-    nstate = s._nstate
-    h2d = ncell * nstate * 8 + ncell * 2 * 8 + nsteps_per * 32
-    d2h = ncell * nstate * 8 + (len(log) - 1) * int(args.step_ms) * 8
+    # Bytes crossing the host boundary per bench step: the state up (the
+    # public call keeps the state on the host between calls, as the
+    # reference does) and the step schedule; the state and frames down
+    nstate = 48
+    h2d = ncell * nstate * 8 + nsteps_per * 40
+    d2h = ncell * nstate * 8 + frame_bytes // max(args.steps, 1)
 
     # Roofline of the tissue kernel (algorithmic bytes per launch)
     bpcs = kernel.bytes_per_cell_step()
@@ -847,121 +1178,76 @@ def run_ours(args):
     per_launch_cs = cell_steps / max(step_launches, 1)
     achieved = bpcs * per_launch_cs / avg_launch_s / 1e9
     peak, peak_kind = read_peaks()
-    traffic = read_traffic()
+    traffic = read_traffic('sheet2048_kahan')
     traffic_per_launch = None
     if traffic and traffic.get('bytes_per_cell_step'):
         traffic_per_launch = traffic['bytes_per_cell_step'] * per_launch_cs
-    # Compute roofline: FP32 lanes x 2 flops x SM clock under load
     sm_mhz = clocks['sm_mhz'] if clocks else 1900.0
-    # Instruction-issue roofline (what binds the L2-resident sheet): warp
-    # instructions per cell-step from the committed ncu capture, against
-    # 4 warp schedulers x 152 SMs issuing one instruction per clock
-    issue = None
-    if traffic and traffic.get('warp_instructions_per_cell_step'):
-        ach = traffic['warp_instructions_per_cell_step'] * value / world
-        peak_i = 4 * 152 * sm_mhz * 1e6
-        issue = {'unit': 'warp instructions/s', 'achieved': ach,
-                 'peak': peak_i, 'frac': ach / peak_i,
-                 'warp_instructions_per_cell_step':
-                     traffic['warp_instructions_per_cell_step'],
-                 'source': traffic.get('source')}
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    issue = issue_roofline(traffic, value / world, sm_mhz, n_sm)
+    fp32_peak = n_sm * 128 * 2 * sm_mhz * 1e6 / 1e12
     flops = kernel.flops_per_cell_step() * value / world / 1e12
 
-    # --- double precision, same sheet --------------------------------------
-    fp64 = None
-    dv = None
-    if args.fp64_steps > 0 and rank == 0:
-        s64, _ = make_sheet(mg.SimulationCUDA, myokit.DOUBLE_PRECISION,
-                            args.size, seed=rank, device=local)
-        logs64 = []
-        d64 = 0.0
-        n64 = 0
-        nrun = args.warmup + args.fp64_steps
-        for i in range(nrun):
-            logs64.append(s64.run(args.step_ms, log=log, log_interval=1))
-            if i >= args.warmup:
-                st = s64.last_run_stats()
-                d64 += st['kernel_ms']
-                n64 += st['cell_steps']
-        fp64 = {'value': n64 / (d64 / 1000.0), 'unit': UNIT,
-                'steps': args.fp64_steps, 'warmup': args.warmup}
-        worst = 0.0
-        for a, b in zip(logs32[:nrun], logs64):
-            for k in a.keys():
-                if k == 'engine.time':
-                    continue
-                worst = max(worst, float(np.max(np.abs(
-                    np.asarray(a[k], dtype=float) -
-                    np.asarray(b[k], dtype=float)))))
-        dv = {'max_abs_dV_mV': worst,
-              'window_ms': nrun * args.step_ms,
-              'against': 'this sheet in double precision on the GPU'}
-        fp64['speedup_fp32_over_fp64'] = value / world / fp64['value']
+    def sheet512():
+        sh = sheet512_runs(args, local, n_sm)
+        tr, v = sh.pop('_issue_inputs')
+        sh['roofline']['issue'] = issue_roofline(tr, v, sm_mhz, n_sm)
+        if sh['roofline']['issue']:
+            sh['roofline']['frac'] = sh['roofline']['issue']['frac']
+        return sh
 
-    # --- single precision with FP64 / Kahan accumulation --------------------
-    variants = {}
-    if args.variant_steps > 0 and rank == 0:
-        for vname, kw in VARIANTS:
-            sv, _ = make_sheet(mg.SimulationCUDA, myokit.SINGLE_PRECISION,
-                               args.size, seed=rank, device=local, **kw)
-            dms = 0.0
-            ncs = 0
-            for i in range(args.warmup + args.variant_steps):
-                flush.fill_(1)
-                torch.cuda.synchronize()
-                sv.run(args.step_ms, log=log, log_interval=1)
-                if i >= args.warmup:
-                    st = sv.last_run_stats()
-                    dms += st['kernel_ms']
-                    ncs += st['cell_steps']
-            v = ncs / (dms / 1000.0)
-            variants[vname] = {
-                'value': v, 'unit': UNIT,
-                'accumulated_states': [x.qname()
-                                       for x in sv.accumulated_states()],
-                'bytes_per_cell_step': sv._last_kernel.bytes_per_cell_step(),
-                'speedup_over_fp64': (v / fp64['value']) if fp64 else None,
-            }
-
-    accuracy = {'fp32_vs_fp64_bench_sheet': dv}
-    if args.accuracy_ms > 0 and rank == 0:
-        accuracy.update(accuracy_runs(args, local))
-
-    adj = None
-    if args.adjoint_ms > 0 and rank == 0:
-        adj = adjoint_runs(args, local)
-
-    others = {}
-    wanted = [c for c in args.configs.split(',') if c and c != 'none']
+    extra = {}
     if rank == 0:
-        for c in wanted:
-            others[c] = {'c1': config_c1, 'c3': config_c3,
-                         'c5': config_c5}[c](args, local)
-
-    cpu = None
-    if not args.no_cpu_baseline and rank == 0:
-        cpu = cpu_baseline(args, myokit.SINGLE_PRECISION, args.cpu_seconds)
+        # Each further measurement reports its own failure instead of
+        # losing the headline line
+        if args.fp64_ms > 0:
+            extra['fp64'] = guarded(c5_fp64, args, local, value / world)
+        if args.s1_ms > 0:
+            extra['accuracy'] = guarded(c5_accuracy, args, local)
+        if args.sheet512_steps > 0:
+            extra['sheet512'] = guarded(sheet512)
+        if args.accuracy_ms > 0:
+            extra['sheet512_accuracy'] = guarded(accuracy_runs, args, local)
+        if args.adjoint_ms > 0:
+            extra['adjoint'] = guarded(adjoint_runs, args, local)
+        others = {}
+        for c in [c for c in args.configs.split(',') if c and c != 'none']:
+            others[c] = guarded({'c1': config_c1, 'c3': config_c3}[c], args,
+                                local)
+        if args.full:
+            others['c5_full'] = guarded(c5_full, args, local)
+        extra['other_configs'] = others
+        if not args.no_cpu_baseline:
+            extra['cpu_baseline'] = guarded(cpu_baseline, args)
 
     if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
         return 0
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
         'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': dev_ms / args.steps, 'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-        'data': 'synthetic (seeded fields and probes)',
-        'config': config(args, 'sheet %dx%d, %d time steps per step' % (
-            args.size, args.size, nsteps_per)),
+        'data': 'synthetic (seeded probes)',
+        'precision': 'FP32 with Kahan-compensated V and concentrations'
+                     ' (%s)' % ', '.join(kernel.states[i].qname()
+                                         for i in kernel.hi_states),
+        'fp32_math': kernel.math,
+        'config': config(args),
+        'timed_window_ms': [t_end - args.steps * args.step_ms, t_end],
+        's2_applied_at_ms': s2_applied[0],
         'e2e': {'value': e2e_value, 'unit': UNIT, 'h2d_bytes_per_step': h2d,
                 'd2h_bytes_per_step': d2h},
         'gpu_launches': launches,
+        'frames_per_step': n_frames / max(args.steps, 1),
         'roofline': {
             'bound': 'hbm', 'achieved': achieved, 'peak': peak,
             'unit': 'GB/s', 'frac': achieved / peak,
             'traffic': traffic_per_launch,
             'peak_source': peak_kind,
             'bytes_per_cell_step': bpcs,
+            'cell_steps_per_launch': per_launch_cs,
+            'traffic_source': traffic and traffic.get('source'),
             'compute': {
                 'unit': 'TFLOP/s', 'achieved': flops, 'peak': fp32_peak,
                 'frac': flops / fp32_peak,
@@ -970,14 +1256,9 @@ def run_ours(args):
                 'peak_source': 'FP32 lanes x 2 x median SM clock'},
             'issue': issue,
         },
-        'fp64': fp64,
-        'variants': variants,
-        'accuracy': accuracy,
-        'adjoint': adj,
-        'other_configs': others,
         'clocks': clocks,
-        'cpu_baseline': cpu,
     }
+    line.update(extra)
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

@@ -277,8 +277,12 @@ int mkg_last_stats(const mkg_sim *sim, double *kernel_ms, int64_t *launches,
  * mkg_run_begin + mkg_run_chunk, keeping a checkpoint every seg_steps steps
  * and all log rows (mkg_adj_read_log, rows x ncol). mkg_adj_backward takes
  * dL/d(log value) (rows x ncol; every column must log V) and writes the
- * field gradients (AoS, ncell x n_field) and dL/dgx, dL/dgy. Homogeneous
- * grid diffusion or none; no accumulation modes.
+ * field gradients (AoS, ncell x n_field) and dL/dgx, dL/dgy. Every
+ * diffusion mode: with per-edge conductances or connections, dL/dgx is the
+ * sum of the x-edge (or connection) gradients and dL/dgy of the y-edge
+ * ones, and mkg_adj_conductance_gradient then gives each edge's gradient.
+ * With an accumulation mode the forward and its recomputation run as the
+ * simulation's own kernel; the reverse sweep runs in the kernel precision.
  */
 int mkg_adj_attach(mkg_sim *sim, const void *cubin, size_t size,
                    int32_t seg_steps);
@@ -287,6 +291,16 @@ int mkg_adj_forward(mkg_sim *sim, double tmin, double tmax, double dt,
 int mkg_adj_read_log(mkg_sim *sim, double *values, int64_t rows);
 int mkg_adj_backward(mkg_sim *sim, const double *lgrad, int64_t rows,
                      double *grad_fields, double *grad_g);
+
+/*
+ * After mkg_adj_backward: dL/dg of every edge. Per-edge conductances
+ * (diff_hetero, openclsim.cl:452-487; layout of sim_init's gx_field and
+ * gy_field, openclsim.py:1380-1384): n = ny*(nx-1) x-edges, then
+ * (ny-1)*nx y-edges in 2D. Connections (diff_arb_step,
+ * openclsim.cl:537-556; the list of mkg_set_connections): n = number of
+ * connections, in their order. Other diffusion modes: MKG_ERR_ARG.
+ */
+int mkg_adj_conductance_gradient(mkg_sim *sim, double *out, int64_t n);
 
 /*
  * Device frame buffer: when set (rows > 0), log rows are written by the

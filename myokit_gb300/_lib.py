@@ -128,6 +128,8 @@ SIGNATURES = {
     'mkg_adj_backward': (ctypes.c_int, [
         ctypes.c_void_p, _c_double_p, ctypes.c_int64, _c_double_p,
         _c_double_p]),
+    'mkg_adj_conductance_gradient': (ctypes.c_int, [
+        ctypes.c_void_p, _c_double_p, ctypes.c_int64]),
     'mkg_stream': (ctypes.c_int, [
         ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     'mkg_schedule_preview': (ctypes.c_int64, [

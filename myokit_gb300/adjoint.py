@@ -186,13 +186,11 @@ class AdjointKernel(object):
     """
     CUDA source for the adjoint of a forward :class:`TissueKernel`: the
     trajectory-writing forward kernel and the reverse kernel, in one module.
-    Supports forward-Euler and Rush-Larsen updates, homogeneous grid
-    diffusion (1D or 2D) or none, and scalar fields.
+    Supports forward-Euler and Rush-Larsen updates, every diffusion mode
+    (homogeneous or per-edge conductances on a 1D or 2D grid, arbitrary
+    connections, none) and scalar fields.
     """
     def __init__(self, fwd, min_blocks=1, threads=None, guards=True):
-        if fwd.diffusion not in (_exp.DIFF_NONE, _exp.DIFF_GRID):
-            raise NotImplementedError(
-                'The adjoint supports homogeneous grid diffusion only.')
         self.fwd = fwd
         self.single = fwd.single
         self.min_blocks = int(min_blocks)
@@ -308,14 +306,14 @@ class AdjointKernel(object):
         for i, s in enumerate(states):
             n = name(s)
             extra = ''
-            if i == fwd.i_vm and fwd.diffusion == _exp.DIFF_GRID:
+            if i == fwd.i_vm and fwd.diffusion != _exp.DIFF_NONE:
                 extra = f' + {A(_exp._IDIFF)} * cdiag'
             out.append(f'{tab}lam[(long long){i} * pitch + cid] = '
                        f'{A(n)}{extra};')
         for k, var in enumerate(fwd.fields):
             out.append(f'{tab}gfield[(long long){k} * pitch + cid] += '
                        f'{A(name(var))};')
-        if fwd.diffusion == _exp.DIFF_GRID:
+        if fwd.diffusion != _exp.DIFF_NONE:
             out.append(f'{tab}mu_out[cid] = {A(_exp._IDIFF)};')
             out.append(f'{tab}gg[cid] += {A(_exp._IDIFF)} * xterm;')
             out.append(f'{tab}gg[pitch + cid] += {A(_exp._IDIFF)} * yterm;')
@@ -330,6 +328,7 @@ class AdjointKernel(object):
             '@LOSS_TARGET@': loss_target,
             '@REVERSE@': '\n'.join(rev),
             '@OUTPUTS@': '\n'.join(out),
+            '@IDIFF_ADJ@': A(_exp._IDIFF),
         }
         text = _exp._read('tissue_adjoint.cu.in')
         for k, v in subs.items():
@@ -363,9 +362,11 @@ class TissueAdjoint(object):
     Forward runs and loss gradients for a :class:`SimulationCUDA`.
 
     ``sim``
-        A simulation with homogeneous grid diffusion (1D or 2D) or none.
-        Its fields are the parameters the gradients refer to; its
-        conductance gives gx, gy. With an accumulation mode the forward
+        A simulation in any diffusion mode: homogeneous conductances gx, gy,
+        per-edge conductances (``set_conductance_field``), connections
+        (``set_connections``) or none. Its fields and its conductances are
+        the parameters the gradients refer to. With an accumulation mode the
+        forward
         runs (and is recomputed) exactly as the simulation's own, FP64 or
         compensated states included; the reverse sweep is in the
         simulation precision and takes the rounding of those states to it
@@ -482,7 +483,15 @@ class TissueAdjoint(object):
         """
         Gradients for ``dl_dv = dL/dV`` at the logged points (the array
         returned by :meth:`forward`). Returns ``{field qname: gradient with
-        the field's shape, 'gx': float, 'gy': float}``.
+        the field's shape, 'gx': ..., 'gy': ...}`` where, by diffusion mode,
+
+        - homogeneous conductances: ``gx`` and ``gy`` are floats;
+        - per-edge conductances: ``gx`` has the shape of the simulation's
+          gx field, ``(ny, nx - 1)`` in 2D or ``(nx - 1,)`` in 1D, and
+          ``gy`` the shape ``(ny - 1, nx)`` (an empty array in 1D);
+        - connections: ``'connections'`` holds one gradient per connection,
+          in the order of the simulation's connection list, and ``gx`` is
+          their sum (``gy`` is 0).
         """
         sim = self.sim
         be = self._prepare()
@@ -502,6 +511,25 @@ class TissueAdjoint(object):
             out[name] = gf[:, k].reshape(shape)
         out['gx'] = float(gg[0])
         out['gy'] = float(gg[1])
+        mode = sim._diffusion_mode()
+        if mode in (_exp.DIFF_HETERO, _exp.DIFF_CONN):
+            nx, ny = sim._nx, sim._ny
+            two_d = len(sim._dims) == 2
+            if mode == _exp.DIFF_HETERO:
+                n = ny * (nx - 1) + ((ny - 1) * nx if two_d else 0)
+            else:
+                n = len(sim._connections)
+            ge = np.zeros(max(n, 1))
+            be.check(be.lib.mkg_adj_conductance_gradient(
+                be.h, _lib.dptr(ge), n))
+            if mode == _exp.DIFF_CONN:
+                out['connections'] = ge[:n]
+            elif two_d:
+                out['gx'] = ge[:ny * (nx - 1)].reshape(ny, nx - 1)
+                out['gy'] = ge[ny * (nx - 1):n].reshape(ny - 1, nx)
+            else:
+                out['gx'] = ge[:n]
+                out['gy'] = np.zeros(0)
         return out
 
     def loss_and_gradient(self, duration, target, log_interval=1.0):
@@ -520,9 +548,17 @@ def _make_function():
         target, g, *fields)``: the sum of squared V errors at the probes of
         a :class:`TissueAdjoint`, as a function of the scalar fields (tensors
         shaped like the grid, in ``adjoint.field_names()`` order) and of the
-        diffusion conductance ``g`` (a scalar tensor: gx = gy = g in 2D, or a
-        two-element tensor (gx, gy)). Gradients come from the discrete
-        adjoint.
+        diffusion conductances ``g``:
+
+        - homogeneous conductances: a scalar tensor (gx = gy = g in 2D) or a
+          two-element tensor (gx, gy);
+        - per-edge conductances: one tensor of the gx field's values
+          followed, in 2D, by the gy field's (the layout of
+          ``set_conductance_field``, flattened);
+        - connections: one tensor of per-connection conductances, in the
+          order of the simulation's connection list.
+
+        Gradients come from the discrete adjoint.
         """
         @staticmethod
         def forward(ctx, adj, duration, log_interval, target, g, *fields):
@@ -530,9 +566,22 @@ def _make_function():
             for name, f in zip(adj.field_names(), fields):
                 sim.set_field(name, f.detach().cpu().double().numpy())
             gv = g.detach().cpu().double().reshape(-1).numpy()
-            gx = float(gv[0])
-            gy = float(gv[1]) if len(gv) > 1 else gx
-            if sim._diffusion_enabled:
+            mode = sim._diffusion_mode()
+            ctx.mode = mode
+            if mode == _exp.DIFF_HETERO:
+                nx, ny = sim._nx, sim._ny
+                n = ny * (nx - 1)
+                if len(sim._dims) == 2:
+                    sim.set_conductance_field(
+                        gv[:n].reshape(ny, nx - 1), gv[n:].reshape(ny - 1, nx))
+                else:
+                    sim.set_conductance_field(gv[:n])
+            elif mode == _exp.DIFF_CONN:
+                sim.set_connections([(i, j, float(x)) for (i, j, _), x in
+                                     zip(sim._connections, gv)])
+            elif sim._diffusion_enabled:
+                gx = float(gv[0])
+                gy = float(gv[1]) if len(gv) > 1 else gx
                 sim.set_conductance(gx, gy)
             v = adj.forward(duration, log_interval)
             tgt = target.detach().cpu().double().numpy() \
@@ -550,7 +599,14 @@ def _make_function():
             adj = ctx.adj
             grads = adj.backward(ctx.lgrad)
             s = float(grad_out)
-            if ctx.g_len > 1:
+            if ctx.mode == _exp.DIFF_HETERO:
+                gg = torch.as_tensor(np.concatenate(
+                    [np.ravel(grads['gx']), np.ravel(grads['gy'])]) * s,
+                    dtype=ctx.g_dtype)
+            elif ctx.mode == _exp.DIFF_CONN:
+                gg = torch.as_tensor(grads['connections'] * s,
+                                     dtype=ctx.g_dtype)
+            elif ctx.g_len > 1:
                 gg = torch.tensor([grads['gx'] * s, grads['gy'] * s],
                                   dtype=ctx.g_dtype)
             else:

@@ -304,6 +304,12 @@ struct mkg_sim {
     int adj_seg = 0;                      /* steps per checkpoint segment */
     void *d_traj = nullptr, *d_lam = nullptr, *d_mu = nullptr;
     void *d_gfield = nullptr, *d_gg = nullptr, *d_lgrad = nullptr;
+    double *d_ge = nullptr;               /* per-edge gradient parts */
+    size_t n_ge = 0;                      /* doubles in d_ge */
+    std::vector<double> h_edge_grad;      /* per-edge / per-connection */
+    long long n_nbr = 0;                  /* CSR entries (2 per connection) */
+    std::vector<int> conn_pos;            /* CSR entries of connection c:
+                                             conn_pos[2c], conn_pos[2c+1] */
     int *d_probe_col = nullptr;
     mkg_step *d_fsteps = nullptr, *d_bsteps = nullptr;
     std::vector<mkg_step> adj_sched;      /* full run, global log rows */
@@ -715,6 +721,7 @@ void mkg_destroy(mkg_sim *s)
     dfree(s->d_mu);
     dfree(s->d_gfield);
     dfree(s->d_gg);
+    dfree(s->d_ge);
     dfree(s->d_lgrad);
     dfree(s->d_probe_col);
     dfree(s->d_fsteps);
@@ -1014,13 +1021,17 @@ int mkg_set_connections(mkg_sim *s, const int64_t *c1, const int64_t *c2,
     std::vector<int> idx(std::max<int64_t>(2 * n, 1));
     std::vector<double> gg(std::max<int64_t>(2 * n, 1));
     /* Each cell's list keeps the order of the connection list. */
+    s->conn_pos.assign(2 * n, 0);
     for (int64_t i = 0; i < n; ++i) {
         const int a = (int)c1[i], b = (int)c2[i];
+        s->conn_pos[2 * i] = fill[a];
         idx[fill[a]] = b;
         gg[fill[a]++] = g[i];
+        s->conn_pos[2 * i + 1] = fill[b];
         idx[fill[b]] = a;
         gg[fill[b]++] = g[i];
     }
+    s->n_nbr = 2 * n;
     dfree(s->d_nbr_ptr);
     dfree(s->d_nbr_idx);
     dfree(s->d_nbr_g);
@@ -1737,10 +1748,6 @@ extern "C" int mkg_adj_attach(mkg_sim *s, const void *cubin, size_t size,
 {
     if (!s || !cubin || !size) return set_err(s, MKG_ERR_ARG, "null argument");
     if (seg_steps < 1) return set_err(s, MKG_ERR_ARG, "seg_steps < 1");
-    if (s->cfg.diffusion != MKG_DIFF_NONE &&
-        s->cfg.diffusion != MKG_DIFF_GRID)
-        return set_err(s, MKG_ERR_ARG,
-                       "the adjoint supports homogeneous grid diffusion");
     if (s->adj_lib) {
         cudaLibraryUnload(s->adj_lib);
         s->adj_lib = nullptr;
@@ -1952,6 +1959,23 @@ int adj_backward(mkg_sim *s, const double *lgrad, int64_t rows,
     CK(s, cudaMemsetAsync(s->d_gfield, 0,
                           plane * std::max(s->cfg.n_field, 1), s->stream));
     CK(s, cudaMemsetAsync(s->d_gg, 0, plane * 2, s->stream));
+    /* Per-edge gradient parts: four per cell on heterogeneous grids, one
+     * per CSR entry with connections */
+    size_t n_ge = 0;
+    if (s->cfg.diffusion == MKG_DIFF_HETERO) n_ge = 4 * (size_t)s->pitch;
+    if (s->cfg.diffusion == MKG_DIFF_CONN) n_ge = (size_t)s->n_nbr;
+    if (n_ge != s->n_ge) {
+        dfree(s->d_ge);
+        s->n_ge = 0;
+        if (n_ge) {
+            CK(s, cudaMalloc((void **)&s->d_ge, n_ge * sizeof(double)));
+            s->n_ge = n_ge;
+        }
+    }
+    if (s->n_ge)
+        CK(s, cudaMemsetAsync(s->d_ge, 0, s->n_ge * sizeof(double),
+                              s->stream));
+    s->h_edge_grad.clear();
     int mu_sel = 0;
     /* The whole schedule on the device, once: the reverse kernel reads the
      * logged rows, the trajectory kernel logs nothing */
@@ -2036,6 +2060,7 @@ int adj_backward(mkg_sim *s, const double *lgrad, int64_t rows,
         b.mu = s->d_mu;
         b.gfield = s->d_gfield;
         b.gg = s->d_gg;
+        b.ge = s->d_ge;
         b.probe_col = s->d_probe_col;
         b.lgrad = s->d_lgrad;
         b.nprobe = ncol;
@@ -2077,10 +2102,62 @@ int adj_backward(mkg_sim *s, const double *lgrad, int64_t rows,
         if (e != cudaSuccess)
             return set_err(s, MKG_ERR_CUDA, "gradient copy failed");
     }
+    /* Per-edge gradients: the two cells' parts of every edge */
+    if (s->n_ge) {
+        std::vector<double> part(s->n_ge);
+        CK(s, cudaMemcpyAsync(part.data(), s->d_ge, s->n_ge * sizeof(double),
+                              cudaMemcpyDeviceToHost, s->stream));
+        CK(s, cudaStreamSynchronize(s->stream));
+        if (s->cfg.diffusion == MKG_DIFF_CONN) {
+            const size_t nc = s->conn_pos.size() / 2;
+            s->h_edge_grad.resize(nc);
+            for (size_t c = 0; c < nc; ++c)
+                s->h_edge_grad[c] = part[s->conn_pos[2 * c]] +
+                                    part[s->conn_pos[2 * c + 1]];
+        } else {
+            /* gx edges (ix, iy)-(ix+1, iy) at iy*(nx-1)+ix: the right part
+             * of the left cell plus the left part of the right cell; gy
+             * edges (ix, iy)-(ix, iy+1) at iy*nx+ix: up part plus down */
+            const long long nx = s->cfg.nx, ny = s->cfg.ny;
+            const long long p = s->pitch;
+            const double *L = part.data(), *R = L + p, *D = R + p, *U = D + p;
+            s->h_edge_grad.clear();
+            for (long long iy = 0; iy < ny; ++iy)
+                for (long long ix = 0; ix + 1 < nx; ++ix) {
+                    const long long c = ix + iy * nx;
+                    s->h_edge_grad.push_back(R[c] + L[c + 1]);
+                }
+            if (s->cfg.two_d)
+                for (long long iy = 0; iy + 1 < ny; ++iy)
+                    for (long long ix = 0; ix < nx; ++ix) {
+                        const long long c = ix + iy * nx;
+                        s->h_edge_grad.push_back(U[c] + D[c + nx]);
+                    }
+        }
+    }
     return MKG_OK;
 }
 
 }  // namespace
+
+extern "C" int mkg_adj_conductance_gradient(mkg_sim *s, double *out,
+                                            int64_t n)
+{
+    if (!s || (n > 0 && !out)) return set_err(s, MKG_ERR_ARG,
+                                              "null argument");
+    if (s->cfg.diffusion != MKG_DIFF_HETERO &&
+        s->cfg.diffusion != MKG_DIFF_CONN)
+        return set_err(s, MKG_ERR_ARG,
+                       "per-edge gradients need per-edge conductances or"
+                       " connections");
+    if (n != (int64_t)s->h_edge_grad.size())
+        return set_err(s, MKG_ERR_ARG,
+                       "expected %lld edge gradients (after"
+                       " mkg_adj_backward)",
+                       (long long)s->h_edge_grad.size());
+    if (n > 0) memcpy(out, s->h_edge_grad.data(), n * sizeof(double));
+    return MKG_OK;
+}
 
 extern "C" int mkg_adj_backward(mkg_sim *s, const double *lgrad,
                                 int64_t rows, double *grad_fields,

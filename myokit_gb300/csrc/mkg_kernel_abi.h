@@ -123,6 +123,11 @@ typedef struct mkg_adj_launch {
     const void *lgrad;       /* Real[rows][nprobe]: dL/dV at logged points */
     int nprobe;
     int mu_sel;              /* plane of mu holding mu_{k+1} at entry */
+    double *ge;              /* per-edge conductance gradient parts, each
+                                cell's own: heterogeneous grids
+                                double[4][pitch] (the edge to the left,
+                                right, down and up neighbour), connections
+                                double[n_nbr] (one per CSR entry) */
 } mkg_adj_launch;
 
 /* Accumulation modes for selected states of a single precision kernel */

@@ -1279,6 +1279,8 @@ class SimulationCUDA(object):
         tmin = self._time
         times = []
         if duration > 0:
+            n0 = _lib.ctypes.c_int64()
+            lib.mkg_launch_count(h, _lib.ctypes.byref(n0))
             self._upload(be)
             items = np.full(self._ntotal, var.index(), dtype=np.int32)
             cells = np.arange(self._ntotal, dtype=np.int64)
@@ -1297,6 +1299,7 @@ class SimulationCUDA(object):
                 status = _lib.MKG_OK
                 ms = 0.0
                 cs = 0
+                nlaunch = 0
                 while status == _lib.MKG_OK:
                     status = be.check(lib.mkg_run_chunk(
                         h, self._chunk_steps(), _lib.ctypes.byref(t_out),
@@ -1307,18 +1310,24 @@ class SimulationCUDA(object):
                                                   None, rows.value))
                         times.append(tt)
                     kms = _lib.ctypes.c_double()
+                    nl = _lib.ctypes.c_int64()
                     ncs = _lib.ctypes.c_int64()
-                    lib.mkg_last_stats(h, _lib.ctypes.byref(kms), None,
+                    lib.mkg_last_stats(h, _lib.ctypes.byref(kms),
+                                       _lib.ctypes.byref(nl),
                                        _lib.ctypes.byref(ncs))
                     ms += kms.value
                     cs += ncs.value
+                    nlaunch += nl.value
             finally:
                 lib.mkg_set_frame_buffer(h, None, 0)
             st = self._host_buffer('state', self._nstate * self._ntotal)
             be.check(lib.mkg_get_state(h, _lib.dptr(st), st.size))
             self._state = st
+            n1 = _lib.ctypes.c_int64()
+            lib.mkg_launch_count(h, _lib.ctypes.byref(n1))
             self._last_stats = {'kernel_ms': ms, 'cell_steps': cs,
-                                'launches': None, 'all_launches': None}
+                                'launches': nlaunch,
+                                'all_launches': n1.value - n0.value}
         self._time += duration
         t = np.concatenate(times) if times else np.zeros(0)
         shape = (len(t), self._ny, self._nx) if len(self._dims) == 2 else (

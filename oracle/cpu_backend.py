@@ -107,6 +107,9 @@ class CpuBackend(object):
         self._lib = None
         self._running = False
         self.threads = _threads()
+        # Time steps per sim_step call (None: the default below); the
+        # benchmark's CPU timing sets it between calls
+        self.chunk_steps = None
 
     # --- helpers ---------------------------------------------------------
 
@@ -250,7 +253,8 @@ class CpuBackend(object):
         if not self._running:
             raise Exception('Simulation not initialized.')
         t = ctypes.c_double()
-        code = self._lib.orc_step(self._steps, ctypes.byref(t))
+        code = self._lib.orc_step(self.chunk_steps or self._steps,
+                                  ctypes.byref(t))
         self._flush_log()
         if code == 0:
             return t.value

@@ -330,3 +330,179 @@ def test_adjoint_with_derivative_references():
         fd = (vals[0] - vals[1]) / (2 * h)
         ad = grads['ina.gNa'][idx]
         assert abs(ad - fd) <= 1e-4 * max(abs(fd), 1e-6 * L), (idx, ad, fd)
+
+
+# ---------------------------------------------------------------------------
+# Per-edge conductances and connections (diff_hetero, openclsim.cl:452-487;
+# diff_arb_step, openclsim.cl:537-556): gradients with respect to every
+# edge's conductance, against central differences of the oracle's loss
+# ---------------------------------------------------------------------------
+
+def _edge_case(kind):
+    """(ncells, setter(sim), parameters {name: (array, index list)})."""
+    rng = np.random.default_rng(21)
+    if kind == 'hetero2d':
+        gx = 9.0 * rng.lognormal(0, 0.2, (5, 5))
+        gy = 6.0 * rng.lognormal(0, 0.2, (4, 6))
+
+        def setter(s, gx=gx, gy=gy):
+            s.set_conductance_field(gx, gy)
+        return (6, 5), setter, {'gx': gx, 'gy': gy}
+    if kind == 'hetero1d':
+        gx = 9.0 * rng.lognormal(0, 0.2, 39)
+
+        def setter(s, gx=gx):
+            s.set_conductance_field(gx)
+        return 40, setter, {'gx': gx}
+    # A chain with a few long-range links
+    n = 30
+    conns = [(i, i + 1, 9.0 * rng.lognormal(0, 0.2)) for i in range(n - 1)]
+    conns += [(0, 12, 2.5), (5, 25, 1.5), (17, 29, 3.0)]
+    g = np.array([c[2] for c in conns])
+
+    def setter(s, g=g):
+        s.set_connections([(i, j, float(x)) for (i, j, _), x in
+                           zip(conns, g)])
+    return n, setter, {'connections': g}
+
+
+def _edge_sim(model, cls, shape, setter, fields):
+    p = myokit.pacing.blocktrain(period=1000, duration=2, offset=1)
+    s = cls(model, p, ncells=shape, precision=DP)
+    if isinstance(shape, tuple):
+        s.set_paced_cells(2, shape[1])
+    else:
+        s.set_paced_cells(3)
+    setter(s)
+    for name, values in fields.items():
+        s.set_field(name, values)
+    return s
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('kind', ['hetero2d', 'hetero1d', 'connections'])
+def test_adjoint_edges_match_oracle_finite_differences(br77, kind):
+    from oracle.refsim import ReferenceCpuSimulation
+    shape, setter, params = _edge_case(kind)
+    fshape = (shape[1], shape[0]) if isinstance(shape, tuple) else (shape,)
+    f0 = _fields(br77, fshape, 1)
+    probes = PROBES if isinstance(shape, tuple) else [0, 7, 20, 29]
+    keys = ['%d.%d.membrane.V' % q if isinstance(q, tuple) else
+            '%d.membrane.V' % q for q in probes]
+    target = np.zeros((24, len(probes))) - 80
+    s = _edge_sim(br77, mg.SimulationCUDA, shape, setter, f0)
+    adj = adjoint.TissueAdjoint(s, probes, segment_steps=70)
+    L, grads = adj.loss_and_gradient(12, target, 0.5)
+
+    def oracle_loss(p):
+        def set_(o):
+            if kind == 'hetero2d':
+                o.set_conductance_field(p['gx'], p['gy'])
+            elif kind == 'hetero1d':
+                o.set_conductance_field(p['gx'])
+            else:
+                setter(o, p['connections'])
+        o = _edge_sim(br77, ReferenceCpuSimulation, shape, set_, f0)
+        d = o.run(12, log=['engine.time'] + keys, log_interval=0.5)
+        v = np.stack([np.asarray(d[k]) for k in keys], axis=1)
+        return float(np.sum((v - target) ** 2))
+
+    assert abs(oracle_loss(params) - L) <= 1e-9 * L
+    rng = np.random.default_rng(8)
+    checked = 0
+    for name, arr in params.items():
+        got = grads[name]
+        assert np.shape(got) == arr.shape
+        for _ in range(4):
+            idx = tuple(int(rng.integers(0, k)) for k in arr.shape)
+            h = 1e-4 * arr[idx]
+            vals = []
+            for sgn in (1, -1):
+                p = {k: v.copy() for k, v in params.items()}
+                p[name][idx] += sgn * h
+                vals.append(oracle_loss(p))
+            fd = (vals[0] - vals[1]) / (2 * h)
+            assert abs(got[idx] - fd) <= 1e-4 * max(abs(fd), 1e-6 * L), (
+                name, idx, got[idx], fd)
+            checked += 1
+    assert checked >= 4
+    # Field gradients are unchanged by the diffusion mode's bookkeeping
+    name = 'isi.gsBar'
+    idx = (0,) * len(fshape)
+    h = 1e-4 * f0[name][idx]
+    vals = []
+    for sgn in (1, -1):
+        f = f0[name].copy()
+        f[idx] += sgn * h
+        s.set_field(name, f)
+        v = adj.forward(12, 0.5)
+        vals.append(float(np.sum((v - target) ** 2)))
+    s.set_field(name, f0[name])
+    fd = (vals[0] - vals[1]) / (2 * h)
+    assert abs(grads[name][idx] - fd) <= 1e-4 * max(abs(fd), 1e-6 * L)
+
+
+@pytest.mark.gpu
+def test_adjoint_uniform_edges_sum_to_homogeneous(br77):
+    # A grid with every x edge 9 and every y edge 6, given as per-edge
+    # conductances: the edge gradients sum to the homogeneous gradients
+    # dL/dgx, dL/dgy, and fields get the same gradients
+    f0 = _fields(br77, (5, 6), 1)
+    target = np.zeros((24, len(PROBES))) - 80
+    out = []
+    for hetero in (False, True):
+        s = _sim(br77, DP, fields=f0)
+        if hetero:
+            s.set_conductance_field(np.full((5, 5), 9.0),
+                                    np.full((4, 6), 6.0))
+        adj = adjoint.TissueAdjoint(s, PROBES, segment_steps=100)
+        out.append(adj.loss_and_gradient(12, target, 0.5))
+    (L0, g0), (L1, g1) = out
+    assert abs(L1 - L0) <= 1e-12 * L0
+    assert abs(np.sum(g1['gx']) - g0['gx']) <= 1e-9 * abs(g0['gx'])
+    assert abs(np.sum(g1['gy']) - g0['gy']) <= 1e-9 * abs(g0['gy'])
+    for k in f0:
+        np.testing.assert_allclose(g1[k], g0[k], rtol=1e-9, atol=1e-12 * L0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('kind', ['hetero2d', 'connections'])
+def test_torch_function_edge_gradients(br77, kind):
+    import torch
+    shape, setter, params = _edge_case(kind)
+    fshape = (shape[1], shape[0]) if isinstance(shape, tuple) else (shape,)
+    f0 = _fields(br77, fshape, 1)
+    probes = PROBES if isinstance(shape, tuple) else [0, 7, 20, 29]
+    s = _edge_sim(br77, mg.SimulationCUDA, shape, setter, f0)
+    adj = adjoint.TissueAdjoint(s, probes, segment_steps=100)
+    target = torch.full((24, len(probes)), -80.0, dtype=torch.float64)
+    flat = np.concatenate([np.ravel(v) for v in params.values()])
+    g = torch.tensor(flat, requires_grad=True)
+    fields = [torch.tensor(f0[n], requires_grad=True)
+              for n in adj.field_names()]
+    loss = adjoint.tissue_loss(adj, 12, target, g, fields, 0.5)
+    loss.backward()
+    L, ref = adj.loss_and_gradient(12, target.numpy(), 0.5)
+    assert abs(loss.item() - L) <= 1e-12 * abs(L)
+    want = np.concatenate([np.ravel(ref[k]) for k in params])
+    np.testing.assert_allclose(g.grad.numpy(), want, rtol=1e-12)
+    for t, n in zip(fields, adj.field_names()):
+        np.testing.assert_allclose(t.grad.numpy(), ref[n], rtol=1e-12)
+
+
+@pytest.mark.parametrize('kind', ['hetero2d', 'hetero1d', 'connections'])
+@pytest.mark.parametrize('precision', [SP, DP])
+def test_adjoint_edge_kernels_compile(br77, kind, precision):
+    shape, setter, params = _edge_case(kind)
+    p = myokit.pacing.blocktrain(period=1000, duration=2, offset=1)
+    s = mg.SimulationCUDA(br77, p, ncells=shape, precision=precision)
+    setter(s)
+    k = s._kernel([])
+    assert k.diffusion == {'hetero2d': 2, 'hetero1d': 2,
+                           'connections': 3}[kind]
+    fwd = exporter.TissueKernel(
+        s._model, s._precision, False, s._bound_variables, [], k.diffusion,
+        k.two_d, [], s._rl_states, k.block, traj=True)
+    ak = adjoint.AdjointKernel(fwd)
+    cubin, _ = _lib.compile_source(ak.source(), ak.options())
+    assert cubin[:4] == b'\x7fELF'

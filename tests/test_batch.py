@@ -99,3 +99,145 @@ def test_frames_to_block(br77):
     assert block.len2d() == 1 and block.shape() == (len(t), 8, 16)
     assert np.array_equal(block.get2d('membrane.V'),
                           f.cpu().double().numpy())
+
+
+# ---------------------------------------------------------------------------
+# Batches against what the reference computes for the same tissues
+# ---------------------------------------------------------------------------
+#
+# The reference expresses a batch of cables as one 1D SimulationOpenCL whose
+# set_connections chains stop at cable ends, with set_paced_cell_list for
+# the first cells of every cable and per-cell set_field values equal to the
+# cable's value (openclsim.py:1387-1449, 1595-1629, 1495-1532). Sheets are
+# expressed the same way: one 1D simulation whose connections form the grid
+# of each sheet. The oracle runs exactly that through the reference's
+# Python layer and its own rendered kernel.
+
+BATCH_FIELDS = ['ina.Gbar', 'ikr.Gbar', 'ik1.Gbar']
+
+
+def _oracle_1d(model, ncell, conns, paced, fields, dt, duration, log):
+    from oracle.refsim import ReferenceCpuSimulation
+    import os
+    s = ReferenceCpuSimulation(model, _p(), ncells=ncell, precision=DP,
+                               rl=True)
+    s.set_threads(os.cpu_count() or 1)
+    s.set_step_size(dt)
+    s.set_connections(conns)
+    s.set_paced_cell_list(paced)
+    for name, values in fields.items():
+        s.set_field(name, values)
+    d = s.run(duration, log=log, log_interval=0.5)
+    return d, np.asarray(s.state(), dtype=float).reshape(ncell, -1)
+
+
+def _cable_case(model):
+    rng = np.random.default_rng(13)
+    lengths = rng.integers(20, 61, 8)
+    fields = {name: model.get(name).eval() * rng.lognormal(0, 0.3, 8)
+              for name in BATCH_FIELDS}
+    starts = np.concatenate([[0], np.cumsum(lengths)[:-1]])
+    conns = [(int(a + k), int(a + k + 1), 10.0)
+             for a, ln in zip(starts, lengths) for k in range(int(ln) - 1)]
+    paced = [int(a + k) for a in starts for k in range(5)]
+    per_cell = {name: np.repeat(v, lengths) for name, v in fields.items()}
+    return lengths, fields, conns, paced, per_cell
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('mode', ['fp64', 'fp64-graphs', 'fp32+kahan'])
+def test_cable_batch_matches_reference_connections(decker, mode):
+    # 8 cables of 20-60 cells, three conductances per cable, the first 5
+    # cells of each paced, dt 0.01 ms over 6 ms (the paced upstroke)
+    lengths, fields, conns, paced, per_cell = _cable_case(decker)
+    n = int(lengths.sum())
+    log = ['engine.time'] + ['%d.membrane.V' % c for c in range(n)]
+    ref, st_ref = _oracle_1d(decker, n, conns, paced, per_cell, 0.01, 6, log)
+    kw = {'precision': DP, 'rl': True}
+    if mode == 'fp64-graphs':
+        kw['steps_per_launch'] = 100     # CUDA-graph chunks, as batched
+    elif mode == 'fp32+kahan':
+        kw = {'precision': SP, 'rl': True, 'accumulate': 'kahan'}
+    b = CableBatch(decker, lengths, _p(), conductance=10.0, paced_cells=5,
+                   fields=fields, **kw)
+    b.sim.set_step_size(0.01)
+    d = b.sim.run(6, log=log, log_interval=0.5)
+    assert np.array_equal(np.asarray(d['engine.time']),
+                          np.asarray(ref['engine.time']))
+    dv = max(float(np.max(np.abs(np.asarray(d[k]) - np.asarray(ref[k]))))
+             for k in log[1:])
+    st = b.sim.state_array().reshape(n, -1)
+    assert max(np.asarray(ref[k]).max() for k in log[1:]) > 0
+    if mode == 'fp32+kahan':
+        assert dv <= 0.5          # mV: the compensated single-precision bar
+    else:
+        assert dv <= 1e-9
+        rel = np.max(np.abs(st - st_ref) / (np.abs(st_ref) + 1e-12))
+        assert rel <= 1e-9
+
+
+@pytest.mark.gpu
+def test_sheet_batch_matches_reference_connections(decker):
+    # Three sheets of uneven size packed in one 2D grid against one 1D
+    # reference simulation whose connections form each sheet's grid
+    shapes = [(40, 12), (33, 20), (17, 7)]
+    g = (9.0, 6.0)
+    vals = {'ina.Gbar': [1.1, 0.8, 1.3], 'ikr.Gbar': [0.7, 1.2, 1.0]}
+    vals = {k: [x * decker.get(k).eval() for x in v] for k, v in vals.items()}
+    offs = np.concatenate([[0], np.cumsum([w * h for w, h in shapes])[:-1]])
+    conns, paced = [], []
+    per_cell = {k: [] for k in vals}
+    for i, ((w, h), o) in enumerate(zip(shapes, offs)):
+        for y in range(h):
+            for x in range(w):
+                c = int(o + x + y * w)
+                if x + 1 < w:
+                    conns.append((c, c + 1, g[0]))
+                if y + 1 < h:
+                    conns.append((c, c + w, g[1]))
+                if x < 3:
+                    paced.append(c)
+        for k in vals:
+            per_cell[k].extend([vals[k][i]] * (w * h))
+    ncell = int(sum(w * h for w, h in shapes))
+    probe = [(0, 0, 0), (0, 39, 11), (1, 16, 10), (1, 32, 19), (2, 8, 6)]
+    okeys = ['%d.membrane.V' % int(offs[i] + x + y * shapes[i][0])
+             for i, x, y in probe]
+    ref, st_ref = _oracle_1d(decker, ncell, conns, paced, per_cell, 0.005,
+                             5, ['engine.time'] + okeys)
+    b = SheetBatch(decker, shapes, _p(), conductance=g, paced_columns=3,
+                   fields=vals, precision=DP, rl=True)
+    bkeys = ['%d.%d.membrane.V' % (b.x0[i] + x, y) for i, x, y in probe]
+    d = b.sim.run(5, log=['engine.time'] + bkeys, log_interval=0.5)
+    for ok, bk in zip(okeys, bkeys):
+        assert np.max(np.abs(np.asarray(d[bk]) - np.asarray(ref[ok]))) \
+            <= 1e-9
+    for i, ((w, h), o) in enumerate(zip(shapes, offs)):
+        one = st_ref[o:o + w * h].reshape(h, w, -1)
+        got = b.sheet_state(i)
+        rel = np.max(np.abs(got - one) / (np.abs(one) + 1e-12))
+        assert rel <= 1e-9, i
+
+
+def test_reference_cable_chains_equal_conductance_field(decker):
+    # In the oracle, the connection chains that express a batch of cables
+    # and the heterogeneous conductances with zeros between cables (the
+    # form CableBatch uses) give the same tissue, bit for bit
+    from oracle.refsim import ReferenceCpuSimulation
+    lengths, fields, conns, paced, per_cell = _cable_case(decker)
+    n = int(lengths.sum())
+    log = ['engine.time'] + ['%d.membrane.V' % c for c in range(0, n, 7)]
+    ref, st_ref = _oracle_1d(decker, n, conns, paced, per_cell, 0.01, 3, log)
+    s = ReferenceCpuSimulation(decker, _p(), ncells=n, precision=DP, rl=True)
+    s.set_step_size(0.01)
+    starts = np.concatenate([[0], np.cumsum(lengths)[:-1]])
+    g = np.full(n - 1, 10.0)
+    g[starts[1:] - 1] = 0
+    s.set_conductance_field(g)
+    s.set_paced_cell_list(paced)
+    for k, v in per_cell.items():
+        s.set_field(k, v)
+    d = s.run(3, log=log, log_interval=0.5)
+    for k in log:
+        assert np.array_equal(np.asarray(d[k]), np.asarray(ref[k])), k
+    assert np.array_equal(np.asarray(s.state()).reshape(n, -1), st_ref)
