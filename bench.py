@@ -212,6 +212,8 @@ def config(args):
         'paced': 'left 4 columns, S1 at 0 ms (2 ms, level 1); lower-left'
                  ' quadrant, S2 at 320 ms',
         'fields': 'none',
+        'fp32_math': 'fast (single precision divisions within the 2.5 ulp'
+                     ' that OpenCL allows; exp, log and pow accurate)',
         'log': 'full V frame every 5 ms (device buffer)',
         'l2': ('inputs larger than L2 (state %.0f MB), no flush' if
                n * n * 48 * 4 > 129e6 else

@@ -91,6 +91,9 @@ typedef struct mkg_config {
                                per CTA is warps x stage x bytes + 128 */
     int32_t v_double;       /* 1: V is stored and updated in FP64 (hi_mode 1
                                with V among the selected states) */
+    int32_t split;          /* warps per warp tile (1, 2 or 4): the kernel
+                               divides each tile's state updates among that
+                               many warps of one CTA (0 is taken as 1) */
 } mkg_config;
 
 /*

@@ -53,6 +53,7 @@ class MkgConfig(ctypes.Structure):
         ('n_hi', ctypes.c_int32),
         ('stage', ctypes.c_int32),
         ('v_double', ctypes.c_int32),
+        ('split', ctypes.c_int32),
     ]
 
 

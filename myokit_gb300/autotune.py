@@ -44,6 +44,12 @@ _CANDIDATES = [
 _CANDIDATES_FP64 = [((128, 1), 1, 0, False, _B), ((256, 1), 1, 0, False, _B),
                     ((64, 1), 1, 0, False, _B), ((32, 1), 1, 0, False, _B),
                     ((256, 1), 1, 0, True, _B), ((256, 1), 1, 0, False, _N)]
+# Grids with fewer warp tiles than SMs: teams of 2 or 4 warps share each
+# tile's work (a sixth entry: warps per tile), one team per CTA or two
+_CANDIDATES_SPLIT = [((64, 1), 1, 0, False, _B, 2),
+                     ((128, 1), 1, 0, False, _B, 4),
+                     ((128, 1), 1, 0, False, _B, 2),
+                     ((256, 1), 1, 0, False, _B, 4)]
 
 
 def _cache_path():
@@ -86,13 +92,21 @@ def lookup(sim):
     return None
 
 
-def _apply(sim, block, min_blocks, spl, lazy=False, sync='barrier'):
+def _apply(sim, block, min_blocks, spl, lazy=False, sync='barrier',
+           split=1):
     sim._block = tuple(block)
     sim._min_blocks = int(min_blocks)
     sim._steps_per_launch = int(spl)
     sim._stage_lazy = int(lazy)
     sim._sync = sync
+    sim._split = int(split)
     sim._graphs = 1
+
+
+def _few_tiles(sim):
+    """True when the grid has fewer warp tiles than a GB300 has SMs."""
+    tiles = -(-sim._nx // 32) * sim._ny
+    return tiles < 152
 
 
 def autotune(sim, duration=None, candidates=None, store=True,
@@ -108,13 +122,16 @@ def autotune(sim, duration=None, candidates=None, store=True,
         # FP64 kernels spill when registers are capped
         candidates = _CANDIDATES_FP64 \
             if sim._precision == myokit.DOUBLE_PRECISION else _CANDIDATES
+        if _few_tiles(sim) and sim._accumulate is None:
+            candidates = list(candidates) + _CANDIDATES_SPLIT
     if duration is None:
         steps = max(20, int(4e8 / sim._ntotal))
         if sim._precision == myokit.DOUBLE_PRECISION:
             steps = max(4, steps // 20)
         duration = steps * sim.step_size()
     saved = (sim._state.copy(), sim._time, sim._block, sim._min_blocks,
-             sim._steps_per_launch, sim._graphs, sim._stage_lazy, sim._sync)
+             sim._steps_per_launch, sim._graphs, sim._stage_lazy, sim._sync,
+             sim._split)
     results = {}
     try:
         for cand in candidates:
@@ -141,6 +158,7 @@ def autotune(sim, duration=None, candidates=None, store=True,
         sim._block, sim._min_blocks = saved[2], saved[3]
         sim._steps_per_launch, sim._graphs = saved[4], saved[5]
         sim._stage_lazy, sim._sync = saved[6], saved[7]
+        sim._split = saved[8]
     if not results:
         return None, results
     best = max(results, key=results.get)
@@ -154,6 +172,7 @@ def autotune(sim, duration=None, candidates=None, store=True,
             'steps_per_launch': best[2],
             'stage_lazy': int(best[3]) if len(best) > 3 else 0,
             'sync': best[4] if len(best) > 4 else 'barrier',
+            'split': best[5] if len(best) > 5 else 1,
             'rate': results[best],
             'when': time.strftime('%Y-%m-%dT%H:%M:%S')}
         try:

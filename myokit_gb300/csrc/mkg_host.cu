@@ -636,12 +636,14 @@ int encode_stage_maps(mkg_sim *s)
     return MKG_OK;
 }
 
-/* CTAs needed to give every warp tile a warp */
+/* CTAs needed to give every warp tile a warp (a team of cfg.split warps
+ * when the kernel divides each tile's work) */
 long long blocks_needed(const mkg_sim *s, const mkg_launch *a)
 {
     const long long nwt = (long long)a->ntiles_x * a->ntiles_y;
     const int threads = s->cfg.block_x * s->cfg.block_y;
-    return (nwt * 32 + threads - 1) / threads;
+    const long long split = s->cfg.split > 1 ? s->cfg.split : 1;
+    return (nwt * 32 * split + threads - 1) / threads;
 }
 
 }  // namespace
@@ -793,6 +795,15 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
         return set_err(nullptr, MKG_ERR_ARG, "v_double needs hi_mode 1");
     if (cfg->stage < 0 || cfg->stage > 2)
         return set_err(nullptr, MKG_ERR_ARG, "stage must be 0, 1 or 2");
+    if (cfg->split < 0 || cfg->split > 4 || cfg->split == 3)
+        return set_err(nullptr, MKG_ERR_ARG, "split must be 1, 2 or 4");
+    if (cfg->split > 1 &&
+        ((cfg->block_x / 32) % cfg->split != 0 ||
+         cfg->block_x / 32 / cfg->split > 15 || cfg->stage ||
+         cfg->hi_mode != MKG_HI_NONE))
+        return set_err(nullptr, MKG_ERR_ARG,
+                       "a split kernel needs whole teams of at most 15 per"
+                       " CTA, no staging and no accumulation planes");
     if (cfg->stage) {
         /* Tensor copy limits: 256 planes per box, int32 coordinates */
         StageLayout L;

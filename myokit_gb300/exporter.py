@@ -184,6 +184,12 @@ class OpCensus(object):
         self.power = 0
         self.cond = 0
 
+    def cost(self):
+        """Estimated instructions: an arithmetic operation 1, a division
+        8, a transcendental function 20, a general power 25."""
+        return (self.arith + 7 * self.divide + 20 * self.trans +
+                25 * self.power)
+
     def add(self, e):
         for x in e.walk():
             if isinstance(x, (myokit.Plus, myokit.Minus, myokit.Multiply,
@@ -396,7 +402,7 @@ class TissueKernel(object):
                  fast_divide=True, min_blocks=1, math='default',
                  accumulate=None, accumulate_states=(), traj=False,
                  stage=False, row_pad=False, stage_lazy=False,
-                 sync='barrier'):
+                 sync='barrier', split=1):
         self.model = model
         self.single = (precision == myokit.SINGLE_PRECISION)
         self.native_math = bool(native_math)
@@ -435,6 +441,23 @@ class TissueKernel(object):
         self.v_double = (self.accumulate == 'double' and
                          self.i_vm in self.hi_index)
         self.traj = bool(traj)
+        # Warps per warp tile (1, 2 or 4). Split teams read their states
+        # themselves and meet at a named CTA barrier, so they take none of
+        # tile staging, accumulation planes, trajectory output or
+        # neighbour synchronisation; where one of those is asked for, or
+        # the CTA does not hold whole teams (at most 15 per CTA: named
+        # barriers 1-15), the kernel is not split.
+        self.split = int(split)
+        if self.split not in (1, 2, 4):
+            raise ValueError('split must be 1, 2 or 4')
+        nwarp = self.block[0] // 32
+        if self.split > 1 and (
+                self.accumulate or self.traj or self.block[1] != 1
+                or nwarp % self.split or nwarp // self.split > 15):
+            self.split = 1
+        if self.split > 1:
+            stage = False
+            sync = 'barrier'
         self.stage = bool(stage)
         self.row_pad = bool(row_pad) and self.two_d
         self.stage_lazy = int(stage_lazy)
@@ -575,6 +598,16 @@ class TissueKernel(object):
                    f'field[(long long){k} * pitch + cid]')
             field_loads.append(
                 f'{tab}const Real {amp}{self._name(var)} = {src};')
+        # (name, referenced names, line, cost) of every equation in body
+        # order, for kernels that divide a tile's work among warps
+        items = []
+
+        def item(lhs, rhs, line):
+            refs = set(self._name(r) for r in rhs.references())
+            c = OpCensus()
+            c.add(rhs)
+            items.append((self._name(lhs), refs, line, c.cost()))
+
         body.append(tab + '// Per-cell constants (scalar fields)')
         for eq in const_eqs:
             var = eq.lhs.var()
@@ -582,8 +615,9 @@ class TissueKernel(object):
                 rhs = fold(eq.rhs)
                 self.cell_const_eqs.append((eq.lhs, rhs))
                 self.census.add(rhs)
-                body.append(
-                    f'{tab}const Real {self._name(var)} = {w.ex(rhs)};')
+                line = f'{tab}const Real {self._name(var)} = {w.ex(rhs)};'
+                body.append(line)
+                item(var, rhs, line)
 
         def ref(var):
             # Name of a variable, or its literal when it was folded
@@ -597,6 +631,7 @@ class TissueKernel(object):
         # state is x - c, updated with Kahan's compensated sum).
         loads = []
         updates = []
+        state_src = []       # (name, value at t) per state, plain loads
         hiD = '((double *)hi)'
         hiR = '((Real *)hi)'
         for i, s in enumerate(self.states):
@@ -612,6 +647,7 @@ class TissueKernel(object):
             else:
                 src = f'state[{plane}]'
                 hsrc = None
+            state_src.append((n, '(Real)V_' if i == self.i_vm else src))
             if i == self.i_vm:
                 loads.append(f'{tab}const Real {n} = (Real)V_;')
             elif j is not None and self.accumulate == 'double':
@@ -699,7 +735,9 @@ class TissueKernel(object):
                 self.rhs_eqs.append((eq.lhs, rhs))
                 self.census.add(rhs)
                 name = self._name(eq.lhs)
-                body.append(f'{tab}const Real {name} = {w.ex(rhs)};')
+                line = f'{tab}const Real {name} = {w.ex(rhs)};'
+                body.append(line)
+                item(eq.lhs, rhs, line)
                 defined.add(name)
                 flush()
         if len(emitted) != len(updates):   # pragma: no cover
@@ -735,7 +773,15 @@ class TissueKernel(object):
                 cond=f'item > {self.n_state}',
                 cases=('\n' + t2 + '        ').join(cases))
 
+        split_body = ''
+        if self.split > 1:
+            split_body = self._split_body(
+                items, updates, state_src, field_loads, log_a, log_b)
+        self.split_body = split_body
+
         subs = {
+            '@SPLIT@': str(self.split),
+            '@SPLIT_BODY@': split_body,
             '@REAL@': real,
             '@VREAL@': 'double' if self.v_double else real,
             '@SINGLE@': '1' if self.single else '0',
@@ -791,6 +837,104 @@ class TissueKernel(object):
         return (
             '// Generated by myokit_gb300.exporter for model '
             + str(m.name()) + '\n' + abi + '\n' + text)
+
+    def _split_body(self, items, updates, state_src, field_loads, log_a,
+                    log_b):
+        """
+        The per-warp code of a split tile: the state updates are divided
+        among the team's warps so that the largest share of work (each
+        update with every equation it needs, counted once per warp that
+        needs it) is small, by greedy assignment from the costliest update
+        down. Warp 0 also logs and checks the NaN halt, so it reads every
+        state and computes the logged intermediaries.
+        """
+        P = self.split
+        refs = {name: r for name, r, _, _ in items}
+        cost = {name: c for name, _, _, c in items}
+
+        def closure(roots):
+            out = set()
+            todo = list(roots)
+            while todo:
+                n = todo.pop()
+                if n in out or n not in refs:
+                    continue
+                out.add(n)
+                todo.extend(refs[n])
+            return out
+
+        # Update texts cost 2 (forward Euler) or an exp and 4 (Rush-Larsen)
+        upd = []
+        for i, need, text in updates:
+            own = 24 if self.states[i] in self.rl_states else 2
+            upd.append((i, need, text, closure(need), own))
+        groups = [set() for _ in range(P)]
+        owns = [0] * P
+        targets = [[] for _ in range(P)]
+        groups[0] |= closure(self._inter_names)
+
+        def gcost(g, extra=frozenset()):
+            return sum(cost[n] for n in groups[g] | extra)
+        for i, need, text, cl, own in sorted(
+                upd, key=lambda u: -(sum(cost[n] for n in u[3]) + u[4])):
+            g = min(range(P), key=lambda g: (gcost(g, cl) + owns[g] + own,
+                                             g))
+            groups[g] |= cl
+            owns[g] += own
+            targets[g].append(i)
+        self.split_costs = [gcost(g) + owns[g] for g in range(P)]
+
+        tab = '            '
+        out = []
+        for p in range(P):
+            mine = set(targets[p])
+            # States read: those the part's equations and updates use
+            read = set(self._name(self.states[i]) for i in mine)
+            for n in groups[p]:
+                read |= refs[n]
+            sts = [(n, src) for n, src in state_src
+                   if p == 0 or n in read]
+            out.append(f'{tab}{"if" if p == 0 else "else if"} (part_ == {p})'
+                       ' {')
+            for n, _ in sts:
+                out.append(f'{tab}    Real {n} = 0;')
+            out.append(f'{tab}    if (live) {{')
+            for n, src in sts:
+                out.append(f'{tab}        {n} = {src};')
+            out.append(f'{tab}    }}')
+            out.append(f'{tab}    // every warp of the team has read the'
+                       ' states at t')
+            out.append(f'{tab}    mkg_team_sync();')
+            out.append(f'{tab}    if (live) {{')
+            out.append(f'{tab}    const Real idiff_ = (Real)id_;')
+            out.append(f'{tab}    (void)idiff_;')
+            out.append(f'{tab}    const Real pace_ = mkg_cell_pace(a, ix, iy,'
+                       ' cid, pace_in);')
+            out.append(f'{tab}    (void)pace_;')
+            out.extend(field_loads)
+            if p == 0:
+                out.append(log_a)
+            defined = set()
+            done = set()
+
+            def flush():
+                for i, need, text, _, _ in upd:
+                    if i in mine and i not in done and need <= defined:
+                        out.append(text)
+                        done.add(i)
+            flush()
+            for name, _, line, _ in items:
+                if name in groups[p]:
+                    out.append(line)
+                    defined.add(name)
+                    flush()
+            if done != mine:   # pragma: no cover
+                raise ValueError('Could not order the state updates.')
+            if p == 0:
+                out.append(log_b)
+            out.append(f'{tab}    }}')
+            out.append(f'{tab}}}')
+        return '\n'.join(out)
 
     # -- public ------------------------------------------------------------
 

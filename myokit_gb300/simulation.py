@@ -257,6 +257,8 @@ class SimulationCUDA(object):
         # Between steps: 'barrier' (grid-wide) or 'neighbors' (each warp
         # waits for the warps whose cells it reads); None: tuned or barrier
         self._sync = None
+        # Warps per warp tile (1, 2 or 4); None: tuned or 1
+        self._split = None
         if accumulate not in (None, 'double', 'kahan'):
             raise ValueError(
                 'The argument "accumulate" must be None, "double" or'
@@ -775,6 +777,16 @@ class SimulationCUDA(object):
                 return hit.get('sync', 'barrier')
         return 'barrier'
 
+    def _split_mode(self):
+        """Warps that share each warp tile's work (1, 2 or 4)."""
+        if self._split is not None:
+            return int(self._split)
+        if self._block is None:
+            hit = self._tuned_choice()
+            if hit is not None:
+                return int(hit.get('split', 1))
+        return 1
+
     def _lazy_staging(self):
         """Staged tiles prefetched into registers (0), or read where used
         from one (1) or two (2) shared-memory buffers per warp."""
@@ -871,7 +883,7 @@ class SimulationCUDA(object):
         key = (
             self._model_version, self._precision, self._native_math, mode,
             two_d, block, minb, self._fp32_math, self._accumulate,
-            stage, row_pad, lazy, self._sync_mode(),
+            stage, row_pad, lazy, self._sync_mode(), self._split_mode(),
             tuple(v.qname() for v in acc),
             tuple(v.qname() for v in self._fields.keys()),
             tuple(v.qname() for v in inter_log))
@@ -884,7 +896,7 @@ class SimulationCUDA(object):
                 min_blocks=minb, math=self._fp32_math,
                 accumulate=self._accumulate, accumulate_states=acc,
                 stage=stage, row_pad=row_pad, stage_lazy=lazy,
-                sync=self._sync_mode())
+                sync=self._sync_mode(), split=self._split_mode())
             if len(self._kernels) > 16:
                 self._kernels.clear()
             self._kernels[key] = k
@@ -910,6 +922,7 @@ class SimulationCUDA(object):
         cfg.n_hi = len(kernel.hi_states)
         cfg.stage = kernel.stage_buffers if kernel.layout else 0
         cfg.v_double = 1 if kernel.v_double else 0
+        cfg.split = kernel.split
         key = (kernel.key(), bytes(cfg))
         if self._backend is not None and self._backend[0] == key:
             return self._backend[1]

@@ -1,0 +1,130 @@
+"""
+Split warp tiles: on grids with fewer warp tiles than SMs, a team of 2 or 4
+warps of one CTA shares each tile's work (every warp updates its own share
+of the states, with the equations those need). The results are those of
+the unsplit kernel (to rounding: the compiler may contract a different set
+of multiply-adds in a part's smaller body) and of the reference.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load, myokit
+import myokit_gb300 as mg
+from myokit_gb300 import _lib
+
+DP = myokit.DOUBLE_PRECISION
+SP = myokit.SINGLE_PRECISION
+
+
+def _cable(model, precision, split, block, rl=False, n=200):
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    s = mg.SimulationCUDA(model, p, ncells=n, precision=precision, rl=rl,
+                          block=block)
+    s._split = split
+    s.set_step_size(0.005)
+    s.set_conductance(9)
+    s.set_paced_cells(5)
+    return s
+
+
+@pytest.mark.parametrize('name,rl', [('beeler-1977-model.mmt', False),
+                                     ('decker-2009.mmt', True),
+                                     ('lr-1991.mmt', False)])
+@pytest.mark.parametrize('split,block', [(2, 64), (4, 128), (4, 256)])
+def test_split_partition_and_compile(name, rl, split, block):
+    # Every state is updated by exactly one warp of the team, the shares
+    # are balanced, and the kernel compiles for sm_103a
+    m = load(name)
+    s = _cable(m, DP, split, block, rl=rl)
+    k = s._kernel([])
+    assert k.split == split
+    src = k.source()
+    assert k.split_body in src
+    for i, st in enumerate(k.states):
+        target = 'vout[cid] =' if i == k.i_vm else \
+            'state[(long long)%d * pitch + cid] =' % i
+        assert k.split_body.count(target) == 1, st.qname()
+    assert k.split_body.count('mkg_team_sync();') == split
+    assert max(k.split_costs) <= 0.7 * sum(k.split_costs)
+    cubin, _ = _lib.compile_source(src, k.options())
+    assert cubin[:4] == b'\x7fELF'
+
+
+def test_split_falls_back_where_unsupported(br77):
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    # Accumulation planes
+    s = mg.SimulationCUDA(br77, p, ncells=100, accumulate='kahan', block=128)
+    s._split = 4
+    assert s._kernel([]).split == 1
+    # A CTA that does not hold whole teams
+    s = mg.SimulationCUDA(br77, p, ncells=100, block=96)
+    s._split = 4
+    assert s._kernel([]).split == 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('split,block', [(2, 64), (4, 128), (4, 256)])
+def test_split_cable200_matches_golden(br77, split, block):
+    # The 200-cell FP64 cable against the reference's Simulation1d
+    g = np.load(os.path.join(GOLDEN, 'br77_cable200_sim1d.npz'))
+    s = _cable(br77, DP, split, block)
+    d = s.run(20, log=['engine.time', 'membrane.V'], log_interval=1).npview()
+    assert s._last_kernel.split == split
+    assert np.max(np.abs(d['engine.time'] - g['engine_time'])) == 0
+    worst = max(np.max(np.abs(d['membrane.V', c] - g['%d_membrane_V' % c]))
+                for c in range(200))
+    assert worst < 1e-9
+
+
+def _same(a, b, rtol):
+    (sa, da), (sb, db) = a, b
+    assert np.allclose(sa, sb, rtol=rtol, atol=0)
+    for k in da.keys():
+        assert np.allclose(np.asarray(da[k]), np.asarray(db[k]), rtol=rtol,
+                           atol=rtol), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('precision', [DP, SP])
+@pytest.mark.parametrize('case', ['cable', 'sheet', 'hetero', 'connections',
+                                  'logged-inter'])
+def test_split_equals_unsplit(decker, precision, case):
+    out = []
+    for split in (1, 2, 4):
+        p = myokit.pacing.blocktrain(period=1000, duration=2, offset=0.5)
+        shape = (70, 6) if case == 'sheet' else 150
+        s = mg.SimulationCUDA(decker, p, ncells=shape, precision=precision,
+                              rl=True, block=128)
+        s._split = split
+        if case == 'sheet':
+            s.set_paced_cells(3, 6)
+        else:
+            s.set_paced_cells(5)
+        if case == 'hetero':
+            s.set_conductance_field(np.linspace(5, 12, 149))
+        elif case == 'connections':
+            s.set_connections([(i, i + 1, 9.0) for i in range(149)] +
+                              [(3, 90, 2.0)])
+        s.set_step_size(0.01)
+        log = ['engine.time', 'membrane.V']
+        if case == 'logged-inter':
+            log += ['ina.INa', 'ical.ICaL']
+        d = s.run(4, log=log, log_interval=0.5)
+        assert s._last_kernel.split == split
+        out.append((s.state_array(), d))
+    rtol = 1e-11 if precision == DP else 2e-4
+    _same(out[0], out[1], rtol)
+    _same(out[0], out[2], rtol)
+
+
+@pytest.mark.gpu
+def test_split_nan_halt():
+    import test_oracle as to
+    s = to.nan_sim(mg.SimulationCUDA)
+    s._block = 128
+    s._split = 4
+    with pytest.raises(myokit.SimulationError, match='Time:  1.23'):
+        s.run(5)
+    assert s._last_kernel.split == 4
