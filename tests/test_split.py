@@ -78,12 +78,17 @@ def test_split_cable200_matches_golden(br77, split, block):
     assert worst < 1e-9
 
 
-def _same(a, b, rtol):
+def _same(a, b, n_state, rtol, vtol):
+    # States: relative to each state's largest magnitude over the cells
+    # (gates and concentrations span many decades); logs: absolute (mV)
     (sa, da), (sb, db) = a, b
-    assert np.allclose(sa, sb, rtol=rtol, atol=0)
+    sa = sa.reshape(-1, n_state)
+    sb = sb.reshape(-1, n_state)
+    scale = np.max(np.abs(sb), axis=0) + 1e-300
+    assert np.max(np.abs(sa - sb) / scale) <= rtol
     for k in da.keys():
-        assert np.allclose(np.asarray(da[k]), np.asarray(db[k]), rtol=rtol,
-                           atol=rtol), k
+        assert np.max(np.abs(np.asarray(da[k], dtype=float) -
+                             np.asarray(db[k], dtype=float))) <= vtol, k
 
 
 @pytest.mark.gpu
@@ -114,9 +119,13 @@ def test_split_equals_unsplit(decker, precision, case):
         d = s.run(4, log=log, log_interval=0.5)
         assert s._last_kernel.split == split
         out.append((s.state_array(), d))
-    rtol = 1e-11 if precision == DP else 2e-4
-    _same(out[0], out[1], rtol)
-    _same(out[0], out[2], rtol)
+    # FP64: rounding only; FP32: the compiler contracts different
+    # multiply-adds in a part's body, and single precision rounding grows
+    # over 400 steps
+    rtol, vtol = (1e-11, 1e-9) if precision == DP else (2e-3, 1e-2)
+    n = decker.count_states()
+    _same(out[0], out[1], n, rtol, vtol)
+    _same(out[0], out[2], n, rtol, vtol)
 
 
 @pytest.mark.gpu
