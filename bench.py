@@ -108,6 +108,9 @@ def parse():
     p.add_argument('--no-fields', action='store_true',
                    help='with --profile: a sheet without scalar fields (the'
                         ' 2048x2048 S1-S2 configuration)')
+    p.add_argument('--profile-cable', action='store_true',
+                   help='with --profile: the 200-cell Beeler-Reuter cable'
+                        ' (--precision, tuned launch shape) instead')
     p.add_argument('--profile-adjoint', action='store_true',
                    help='with --profile: run the discrete adjoint (loss on'
                         ' 64 probes, checkpoints every 200 steps) instead')
@@ -1032,6 +1035,28 @@ def profile_case(args):
     prec = myokit.DOUBLE_PRECISION if args.precision == 'double' \
         else myokit.SINGLE_PRECISION
     acc = None if args.accumulate == 'none' else args.accumulate
+    if args.profile_cable:
+        path = os.path.join(os.path.dirname(myokit.__file__), 'tests',
+                            'data', 'beeler-1977-model.mmt')
+        p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+        s = mg.SimulationCUDA(myokit.load_model(path), p, ncells=200,
+                              precision=prec, accumulate=acc)
+        s.set_step_size(0.005)
+        s.set_conductance(9)
+        s.set_paced_cells(5)
+        s._steps_per_launch = args.profile_steps
+        ms = args.profile_steps * 0.005
+        for _ in range(2):
+            s.run(ms, log=['engine.time'], log_interval=1)
+        st = s.last_run_stats()
+        k = s._last_kernel
+        print(json.dumps({'cable': 200, 'precision': args.precision,
+                          'block': k.block[0], 'split': k.split,
+                          'launches': st['launches'],
+                          'kernel_ms': st['kernel_ms'],
+                          'cell_steps_per_s': st['cell_steps'] /
+                          (st['kernel_ms'] / 1000)}))
+        return 0
     if args.profile_adjoint:
         from myokit_gb300 import adjoint as ad
         s, _ = make_sheet(mg.SimulationCUDA, prec, args.size,
