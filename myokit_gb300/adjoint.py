@@ -217,7 +217,8 @@ class AdjointKernel(object):
         for lhs, rhs in fwd.cell_const_eqs:
             fw.append(f'{tab}const Real {name(lhs)} = {w.ex(rhs)};')
         for lhs, rhs in fwd.rhs_eqs:
-            fw.append(f'{tab}const Real {name(lhs)} = {w.ex(rhs)};')
+            fw.append(f'{tab}const Real {name(lhs)} = '
+                      f'{fwd.rhs_code(lhs, rhs)};')
 
         # Adjoint accumulators: every state, field, per-cell constant,
         # equation left-hand side and the diffusion current
@@ -271,6 +272,21 @@ class AdjointKernel(object):
         for lhs, rhs in reversed(fwd.rhs_eqs + []):
             a = A(name(lhs))
             terms = []
+            bcd = fwd.cubic.get(name(lhs))
+            if bcd is not None:
+                # A refined root x of x^3 + b x^2 + c x + d: by the implicit
+                # function theorem dx/db = -x^2/g, dx/dc = -x/g, dx/dd = -1/g
+                # with g = 3x^2 + 2bx + c
+                x = name(lhs)
+                b, c, d = bcd
+                terms.append(f'{tab}    const Real g_ = (3 * {x} + 2 * {b})'
+                             f' * {x} + {c};')
+                terms.append(f'{tab}    const Real r_ = (g_ != 0) ? a_ / g_'
+                             ' : (Real)0;')
+                for rn, dx in ((b, f'{x} * {x}'), (c, x), (d, '1')):
+                    if rn in valid:
+                        terms.append(f'{tab}    {A(rn)} -= r_ * ({dx});')
+                rhs = myokit.Number(0)   # no further terms
             for r in _references(rhs):
                 rn = name(r)
                 if rn in (_exp._T, _exp._PACE):

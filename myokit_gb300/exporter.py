@@ -76,12 +76,15 @@ class CudaExpressionWriter(CBasedExpressionWriter):
     counterpart of OpenCL's ``native_*`` functions
     (``myokit/formats/opencl/_ewriter.py:59-93``).
     """
-    def __init__(self, single, native_math=False, fast_divide=False):
+    def __init__(self, single, native_math=False, fast_divide=False,
+                 exp64=False):
         super().__init__()
         self._single = bool(single)
         self._native = bool(native_math) and self._single
         self._fast_div = bool(fast_divide) and self._single
         self.int_powers = set()
+        # Double precision: exp through mkg_exp64 (_exp64_helper)
+        self._exp64 = bool(exp64) and not self._single
 
     def _ex_divide(self, e):
         if not self._fast_div:
@@ -99,7 +102,7 @@ class CudaExpressionWriter(CBasedExpressionWriter):
 
     def _fn(self, name):
         if not self._single:
-            return name
+            return 'mkg_exp64' if name == 'exp' and self._exp64 else name
         if self._native and name in ('exp', 'log', 'sin', 'cos', 'tan',
                                      'log10'):
             return '__' + name + 'f'
@@ -240,8 +243,155 @@ _LOG_BLOCK = '''
         }}'''
 
 
+def _exp64_helper():
+    """
+    CUDA source of mkg_exp64, a double precision exp by Tang's
+    table-driven method (P. T. P. Tang, "Table-driven implementation of the
+    exponential function in IEEE floating-point arithmetic", ACM Trans.
+    Math. Softw. 15(2), 1989): x = (32 m + j) ln2/32 + r with |r| <= ln2/64;
+    exp(x) = 2^m 2^(j/32) exp(r), with 2^(j/32) from a table as the sum of
+    two doubles and exp(r) - 1 from its Taylor polynomial to degree 6
+    (truncation below 4e-18 relative). The constants are computed here in
+    60-digit decimal arithmetic. Arguments outside (-700, 700), and NaN,
+    go to CUDA's exp in a function that is not inlined, so that the common
+    path carries no second exp. GB300 issues double precision instructions
+    at a small fraction of the single precision rate; this path takes 11 of
+    them.
+    """
+    from decimal import Decimal, localcontext
+    import struct
+    with localcontext() as ctx:
+        ctx.prec = 60
+        ln2 = Decimal(2).ln()
+        step = ln2 / 32
+        # ln2/32 as L1 + L2, L1 with 21 trailing zero bits so that N * L1
+        # is exact for |N| < 2^21
+        bits = struct.unpack('<Q', struct.pack('<d', float(step)))[0]
+        l1 = struct.unpack('<d', struct.pack(
+            '<Q', bits & ~((1 << 21) - 1)))[0]
+        l2 = float(step - Decimal(l1))
+        inv = float(Decimal(32) / ln2)
+        tab = []
+        for j in range(32):
+            t = (Decimal(j) * step).exp()
+            hi = float(t)
+            tab += [hi, float(t - Decimal(hi))]
+        coef = []
+        f = 1
+        for k in range(2, 7):
+            f *= k
+            coef.append(float(Decimal(1) / f))
+    h = float.hex
+    rows = ',\n    '.join(', '.join(h(v) for v in tab[i:i + 4])
+                          for i in range(0, 64, 4))
+    return f'''
+// 2^(j/32) as hi + lo doubles, j = 0..31 (mkg_exp64)
+static __device__ __align__(16) const double mkg_exp_tab[64] = {{
+    {rows}}};
+
+// Arguments outside the table method's range
+static __device__ __noinline__ double mkg_exp64_wide(double x)
+{{
+    return exp(x);
+}}
+
+// exp(x), double precision, by Tang's table-driven method (see the
+// exporter's _exp64_helper); within one ulp of the exact value
+static __device__ __forceinline__ double mkg_exp64(double x)
+{{
+    if (!(fabs(x) < 700.0)) return mkg_exp64_wide(x);
+    // n = round(x * 32 / ln2) in the low word of t (shifter 1.5 * 2^52)
+    const double t = fma(x, {h(inv)}, 0x1.8p+52);
+    const int n = __double2loint(t);
+    const double N = t - 0x1.8p+52;
+    double r = fma(-N, {h(l1)}, x);
+    r = fma(-N, {h(l2)}, r);
+    double q = fma(r, {h(coef[4])}, {h(coef[3])});
+    q = fma(q, r, {h(coef[2])});
+    q = fma(q, r, {h(coef[1])});
+    q = fma(q, r, {h(coef[0])});
+    const double p = fma(r * r, q, r);                 // exp(r) - 1
+    const double2 T = __ldg((const double2 *)mkg_exp_tab + (n & 31));
+    const double y = T.x + fma(T.x, p, T.y);           // 2^(j/32) exp(r)
+    // times 2^m, m = n >> 5, in the exponent field (y and the result are
+    // normal for |x| < 700)
+    return __hiloint2double(__double2hiint(y) + ((n >> 5) << 20),
+                            __double2loint(y));
+}}
+'''
+
+
+_CUBIC_HELPER = '''
+// Two Newton steps on x^3 + b x^2 + c x + d = 0 from the estimate x: a
+// root given by the trigonometric cubic formula differs from the sum of
+// two nearly equal terms, which keeps few correct digits in single
+// precision; two steps restore them (see cubic_root_coefficients)
+static __device__ __forceinline__ Real mkg_cubic_root(Real x, Real b, Real c,
+                                                      Real d)
+{
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const Real f = ((x + b) * x + c) * x + d;
+        const Real g = (3 * x + 2 * b) * x + c;
+        if (g != 0) x = x - f / g;
+    }
+    return x;
+}'''
+
+
+def cubic_root_coefficients(rhs):
+    """
+    If ``rhs`` computes a root of ``x^3 + b x^2 + c x + d`` from three
+    referenced variables (b, c, d) by a closed formula with ``acos`` and
+    ``sqrt`` (the trigonometric solution some buffering models use for a
+    free concentration), returns their references ``(b, c, d)``; else None.
+    Detected numerically: for each assignment of the three references, the
+    expression must return a root of test cubics with three real roots.
+    """
+    import itertools
+    import warnings
+    kinds = set(type(x) for x in rhs.walk())
+    if myokit.ACos not in kinds or myokit.Sqrt not in kinds:
+        return None
+    refs = []
+    for r in rhs.references():
+        if r not in refs:
+            refs.append(r)
+    if len(refs) != 3 or not all(isinstance(r, myokit.Name) for r in refs):
+        return None
+    tests = [(1e-4, -0.05, -0.3), (2e-3, -0.01, -0.7), (0.5, -1.0, -2.0),
+             (3.0, 1.0, -4.0), (2.5e-7, -0.003, -0.04)]
+    for perm in itertools.permutations(refs):
+        ok = True
+        for r1, r2, r3 in tests:
+            b = -(r1 + r2 + r3)
+            c = r1 * r2 + r1 * r3 + r2 * r3
+            d = -r1 * r2 * r3
+            sub = {perm[0]: myokit.Number(b), perm[1]: myokit.Number(c),
+                   perm[2]: myokit.Number(d)}
+            try:
+                with np.errstate(all='ignore'), warnings.catch_warnings():
+                    warnings.simplefilter('ignore')
+                    x = rhs.eval(subst=sub)
+                x = float(x) if np.isreal(x) else float('nan')
+            except Exception:
+                ok = False
+                break
+            # Constants folded in single precision (2/3 and the like) move
+            # the formula's value by a few parts in 1e8 of the roots' scale
+            scale = max(abs(r1), abs(r2), abs(r3))
+            if not (np.isfinite(x) and min(abs(x - r) for r in (r1, r2, r3))
+                    <= 1e-5 * scale):
+                ok = False
+                break
+        if ok:
+            return tuple(perm)
+    return None
+
+
 def _pow_helpers(single):
-    """Inline helpers for x^n (n = 2..16, by repeated squaring) and x^1.5."""
+    """Inline helpers for x^n (n = 2..16, by repeated squaring) and x^1.5
+    and, in single precision, the cubic root refinement."""
     out = []
     for n in range(2, 17):
         lines = []
@@ -263,6 +413,10 @@ def _pow_helpers(single):
     sq = 'sqrtf' if single else 'sqrt'
     out.append('static __device__ __forceinline__ Real mkg_pow1p5(Real x)'
                f' {{ return x * {sq}(x); }}')
+    if single:
+        out.append(_CUBIC_HELPER)
+    else:
+        out.append(_exp64_helper())
     return '\n'.join(out)
 
 
@@ -402,7 +556,7 @@ class TissueKernel(object):
                  fast_divide=True, min_blocks=1, math='default',
                  accumulate=None, accumulate_states=(), traj=False,
                  stage=False, row_pad=False, stage_lazy=False,
-                 sync='barrier', split=1):
+                 sync='barrier', split=1, exp64=True):
         self.model = model
         self.single = (precision == myokit.SINGLE_PRECISION)
         self.native_math = bool(native_math)
@@ -419,6 +573,8 @@ class TissueKernel(object):
         self.fast_divide = (bool(fast_divide) and self.single
                             and self.math != 'ieee')
         self.min_blocks = int(min_blocks)
+        # Double precision: exp by the table method (_exp64_helper)
+        self.exp64 = bool(exp64) and not self.single
         self.states = list(model.states())
         self.n_state = len(self.states)
         self.vm = model.label('membrane_potential')
@@ -491,6 +647,9 @@ class TissueKernel(object):
         self.stage_buffers = 2 if self.layout and self.stage_lazy == 2 \
             else 1
         self.census = OpCensus()
+        # Single precision: variables computed by the trigonometric cubic
+        # formula, refined by mkg_cubic_root: name -> (b, c, d) names
+        self.cubic = {}
         self._source = self._generate()
 
     # -- naming ------------------------------------------------------------
@@ -517,7 +676,7 @@ class TissueKernel(object):
     def _generate(self):
         m = self.model
         w = CudaExpressionWriter(self.single, self.native_math,
-                                 self.math == 'fast')
+                                 self.math == 'fast', exp64=self.exp64)
         w.set_lhs_function(self._name)
         real = 'float' if self.single else 'double'
         prec = myokit.SINGLE_PRECISION if self.single else \
@@ -735,7 +894,12 @@ class TissueKernel(object):
                 self.rhs_eqs.append((eq.lhs, rhs))
                 self.census.add(rhs)
                 name = self._name(eq.lhs)
-                line = f'{tab}const Real {name} = {w.ex(rhs)};'
+                if self.single and isinstance(eq.lhs, myokit.Name):
+                    bcd = cubic_root_coefficients(rhs)
+                    if bcd is not None:
+                        self.cubic[name] = tuple(self._name(r) for r in bcd)
+                        self.census.arith += 20
+                line = f'{tab}const Real {name} = {self.rhs_code(eq.lhs, rhs)};'
                 body.append(line)
                 item(eq.lhs, rhs, line)
                 defined.add(name)
@@ -935,6 +1099,15 @@ class TissueKernel(object):
             out.append(f'{tab}    }}')
             out.append(f'{tab}}}')
         return '\n'.join(out)
+
+    def rhs_code(self, lhs, rhs):
+        """CUDA expression for an equation's right-hand side, with the
+        cubic root refinement where it applies."""
+        text = self.writer.ex(rhs)
+        bcd = self.cubic.get(self._name(lhs))
+        if bcd is not None:
+            text = f'mkg_cubic_root({text}, {bcd[0]}, {bcd[1]}, {bcd[2]})'
+        return text
 
     # -- public ------------------------------------------------------------
 

@@ -103,3 +103,33 @@ def test_census_counts_work():
     assert k.bytes_per_cell_step() == 2 * 48 * 4
     k = _kernel(load('beeler-1977-model.mmt'), 10, DP)
     assert k.bytes_per_cell_step() == 2 * 8 * 8
+
+
+def test_cubic_root_refinement_single_precision_only():
+    # Decker 2009 computes free Ca_i, Ca_sr and Ca_cal with the
+    # trigonometric solution of a cubic; single precision kernels refine
+    # each with Newton steps on that cubic, double precision kernels keep
+    # the reference's expressions
+    from myokit_gb300.exporter import cubic_root_coefficients
+    m = load('decker-2009.mmt')
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    ks = {}
+    for prec in (myokit.SINGLE_PRECISION, myokit.DOUBLE_PRECISION):
+        s = mg.SimulationCUDA(m, p, ncells=64, precision=prec, rl=True)
+        ks[prec] = s._kernel([])
+    k = ks[myokit.SINGLE_PRECISION]
+    assert sorted(k.cubic) == ['v_Ca_cal', 'v_Ca_i', 'v_Ca_sr']
+    assert k.cubic['v_Ca_i'] == ('v_calciumb_Ca_i_b', 'v_calciumb_Ca_i_c',
+                                 'v_calciumb_Ca_i_d')
+    assert 'v_Ca_i = mkg_cubic_root(' in k.source()
+    assert ks[myokit.DOUBLE_PRECISION].cubic == {}
+    assert 'mkg_cubic_root(' not in ks[myokit.DOUBLE_PRECISION].source()
+    # Not a cubic root: other expressions with acos and sqrt
+    x = myokit.Name(m.get('calciumb.Ca_i.b'))
+    y = myokit.Name(m.get('calciumb.Ca_i.c'))
+    z = myokit.Name(m.get('calciumb.Ca_i.d'))
+    e = myokit.Plus(myokit.ACos(myokit.Divide(x, myokit.Number(10))),
+                    myokit.Sqrt(myokit.Plus(myokit.Multiply(y, y),
+                                            myokit.Multiply(z, z))))
+    assert cubic_root_coefficients(e) is None
+    assert cubic_root_coefficients(m.get('ina.INa').rhs()) is None

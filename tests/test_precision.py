@@ -106,3 +106,39 @@ def test_metrics_on_synthetic_action_potential():
     apd = metrics.apd90(t, v)
     # 90% repolarisation: exp(-(t-12)/80) = 0.1
     assert abs(apd - (12 + 80 * np.log(10) - (10 + 2 * 55 / 125))) < 0.5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('acc', [None, 'kahan'])
+def test_conduction_drift_along_a_long_cable(acc):
+    # A wave crossing 1000 Decker cells (one row of the paced-edge sheet):
+    # single precision must not change the conduction velocity. Free Ca
+    # from the trigonometric cubic formula loses most of its single
+    # precision digits with a systematic bias; refined by Newton steps on
+    # the cubic (exporter.cubic_root_coefficients) the activation times
+    # stay within a microsecond of FP64 (with the formula alone they drift
+    # by several, growing with distance).
+    import bench
+    n = 1000
+    xs = list(range(0, n, 50)) + [n - 1]
+    log = ['engine.time'] + ['%d.membrane.V' % x for x in xs]
+    out = []
+    for prec, kw in ((DP, {}), (SP, {'accumulate': acc})):
+        s = bench.make_s1_cable(mg.SimulationCUDA, prec, n, **kw)
+        if prec == SP:
+            assert len(s._kernel([]).cubic) == 3
+        out.append(s.run(220, log=log, log_interval=0.1))
+    ref, got = out
+    t = np.asarray(ref['engine.time'])
+    errs = []
+    for k in log[1:]:
+        a = metrics.activation_time(t, np.asarray(got[k], dtype=float))
+        b = metrics.activation_time(t, np.asarray(ref[k], dtype=float))
+        assert np.isfinite(a) and np.isfinite(b), k
+        errs.append(abs(a - b))
+    assert max(errs) <= 1e-3          # ms
+    c = metrics.compare(t, {k: np.asarray(got[k], dtype=float)
+                            for k in log[1:]},
+                        {k: np.asarray(ref[k], dtype=float)
+                         for k in log[1:]})
+    assert c['max_abs_dV_mV'] <= 0.5
