@@ -108,9 +108,6 @@ def parse():
     p.add_argument('--no-fields', action='store_true',
                    help='with --profile: a sheet without scalar fields (the'
                         ' 2048x2048 S1-S2 configuration)')
-    p.add_argument('--cuda-exp64', action='store_true',
-                   help='with --profile: double precision kernels call'
-                        ' CUDA\'s exp instead of the table method')
     p.add_argument('--profile-cable', action='store_true',
                    help='with --profile: the 200-cell Beeler-Reuter cable'
                         ' (--precision, tuned launch shape) instead')
@@ -1048,7 +1045,6 @@ def profile_case(args):
         s.set_conductance(9)
         s.set_paced_cells(5)
         s._steps_per_launch = args.profile_steps
-        s._exp64 = not args.cuda_exp64
         ms = args.profile_steps * 0.005
         for _ in range(2):
             s.run(ms, log=['engine.time'], log_interval=1)
@@ -1056,7 +1052,6 @@ def profile_case(args):
         k = s._last_kernel
         print(json.dumps({'cable': 200, 'precision': args.precision,
                           'block': k.block[0], 'split': k.split,
-                          'exp64': 'cuda' if args.cuda_exp64 else 'table',
                           'launches': st['launches'],
                           'kernel_ms': st['kernel_ms'],
                           'cell_steps_per_s': st['cell_steps'] /
@@ -1096,7 +1091,6 @@ def profile_case(args):
                         fields=not args.no_fields,
                         steps_per_launch=args.profile_steps, accumulate=acc,
                         stage_tiles=not args.no_stage)
-    s._exp64 = not args.cuda_exp64
     ms = args.profile_steps * 0.005
     for _ in range(2):
         s.run(ms, log=log, log_interval=1)

@@ -76,15 +76,12 @@ class CudaExpressionWriter(CBasedExpressionWriter):
     counterpart of OpenCL's ``native_*`` functions
     (``myokit/formats/opencl/_ewriter.py:59-93``).
     """
-    def __init__(self, single, native_math=False, fast_divide=False,
-                 exp64=False):
+    def __init__(self, single, native_math=False, fast_divide=False):
         super().__init__()
         self._single = bool(single)
         self._native = bool(native_math) and self._single
         self._fast_div = bool(fast_divide) and self._single
         self.int_powers = set()
-        # Double precision: exp through mkg_exp64 (_exp64_helper)
-        self._exp64 = bool(exp64) and not self._single
 
     def _ex_divide(self, e):
         if not self._fast_div:
@@ -102,7 +99,7 @@ class CudaExpressionWriter(CBasedExpressionWriter):
 
     def _fn(self, name):
         if not self._single:
-            return 'mkg_exp64' if name == 'exp' and self._exp64 else name
+            return name
         if self._native and name in ('exp', 'log', 'sin', 'cos', 'tan',
                                      'log10'):
             return '__' + name + 'f'
@@ -243,84 +240,6 @@ _LOG_BLOCK = '''
         }}'''
 
 
-def _exp64_helper():
-    """
-    CUDA source of mkg_exp64, a double precision exp by Tang's
-    table-driven method (P. T. P. Tang, "Table-driven implementation of the
-    exponential function in IEEE floating-point arithmetic", ACM Trans.
-    Math. Softw. 15(2), 1989): x = (32 m + j) ln2/32 + r with |r| <= ln2/64;
-    exp(x) = 2^m 2^(j/32) exp(r), with 2^(j/32) from a table as the sum of
-    two doubles and exp(r) - 1 from its Taylor polynomial to degree 6
-    (truncation below 4e-18 relative). The constants are computed here in
-    60-digit decimal arithmetic. Arguments outside (-700, 700), and NaN,
-    go to CUDA's exp in a function that is not inlined, so that the common
-    path carries no second exp. GB300 issues double precision instructions
-    at a small fraction of the single precision rate; this path takes 11 of
-    them.
-    """
-    from decimal import Decimal, localcontext
-    import struct
-    with localcontext() as ctx:
-        ctx.prec = 60
-        ln2 = Decimal(2).ln()
-        step = ln2 / 32
-        # ln2/32 as L1 + L2, L1 with 21 trailing zero bits so that N * L1
-        # is exact for |N| < 2^21
-        bits = struct.unpack('<Q', struct.pack('<d', float(step)))[0]
-        l1 = struct.unpack('<d', struct.pack(
-            '<Q', bits & ~((1 << 21) - 1)))[0]
-        l2 = float(step - Decimal(l1))
-        inv = float(Decimal(32) / ln2)
-        tab = []
-        for j in range(32):
-            t = (Decimal(j) * step).exp()
-            hi = float(t)
-            tab += [hi, float(t - Decimal(hi))]
-        coef = []
-        f = 1
-        for k in range(2, 7):
-            f *= k
-            coef.append(float(Decimal(1) / f))
-    h = float.hex
-    rows = ',\n    '.join(', '.join(h(v) for v in tab[i:i + 4])
-                          for i in range(0, 64, 4))
-    return f'''
-// 2^(j/32) as hi + lo doubles, j = 0..31 (mkg_exp64)
-static __device__ __align__(16) const double mkg_exp_tab[64] = {{
-    {rows}}};
-
-// Arguments outside the table method's range
-static __device__ __noinline__ double mkg_exp64_wide(double x)
-{{
-    return exp(x);
-}}
-
-// exp(x), double precision, by Tang's table-driven method (see the
-// exporter's _exp64_helper); within one ulp of the exact value
-static __device__ __forceinline__ double mkg_exp64(double x)
-{{
-    if (!(fabs(x) < 700.0)) return mkg_exp64_wide(x);
-    // n = round(x * 32 / ln2) in the low word of t (shifter 1.5 * 2^52)
-    const double t = fma(x, {h(inv)}, 0x1.8p+52);
-    const int n = __double2loint(t);
-    const double N = t - 0x1.8p+52;
-    double r = fma(-N, {h(l1)}, x);
-    r = fma(-N, {h(l2)}, r);
-    double q = fma(r, {h(coef[4])}, {h(coef[3])});
-    q = fma(q, r, {h(coef[2])});
-    q = fma(q, r, {h(coef[1])});
-    q = fma(q, r, {h(coef[0])});
-    const double p = fma(r * r, q, r);                 // exp(r) - 1
-    const double2 T = __ldg((const double2 *)mkg_exp_tab + (n & 31));
-    const double y = T.x + fma(T.x, p, T.y);           // 2^(j/32) exp(r)
-    // times 2^m, m = n >> 5, in the exponent field (y and the result are
-    // normal for |x| < 700)
-    return __hiloint2double(__double2hiint(y) + ((n >> 5) << 20),
-                            __double2loint(y));
-}}
-'''
-
-
 _CUBIC_HELPER = '''
 // Two Newton steps on x^3 + b x^2 + c x + d = 0 from the estimate x: a
 // root given by the trigonometric cubic formula differs from the sum of
@@ -415,8 +334,6 @@ def _pow_helpers(single):
                f' {{ return x * {sq}(x); }}')
     if single:
         out.append(_CUBIC_HELPER)
-    else:
-        out.append(_exp64_helper())
     return '\n'.join(out)
 
 
@@ -556,7 +473,7 @@ class TissueKernel(object):
                  fast_divide=True, min_blocks=1, math='default',
                  accumulate=None, accumulate_states=(), traj=False,
                  stage=False, row_pad=False, stage_lazy=False,
-                 sync='barrier', split=1, exp64=True):
+                 sync='barrier', split=1):
         self.model = model
         self.single = (precision == myokit.SINGLE_PRECISION)
         self.native_math = bool(native_math)
@@ -573,8 +490,6 @@ class TissueKernel(object):
         self.fast_divide = (bool(fast_divide) and self.single
                             and self.math != 'ieee')
         self.min_blocks = int(min_blocks)
-        # Double precision: exp by the table method (_exp64_helper)
-        self.exp64 = bool(exp64) and not self.single
         self.states = list(model.states())
         self.n_state = len(self.states)
         self.vm = model.label('membrane_potential')
@@ -676,7 +591,7 @@ class TissueKernel(object):
     def _generate(self):
         m = self.model
         w = CudaExpressionWriter(self.single, self.native_math,
-                                 self.math == 'fast', exp64=self.exp64)
+                                 self.math == 'fast')
         w.set_lhs_function(self._name)
         real = 'float' if self.single else 'double'
         prec = myokit.SINGLE_PRECISION if self.single else \

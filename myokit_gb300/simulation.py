@@ -259,8 +259,6 @@ class SimulationCUDA(object):
         self._sync = None
         # Warps per warp tile (1, 2 or 4); None: tuned or 1
         self._split = None
-        # Double precision exp by the table method (exporter._exp64_helper)
-        self._exp64 = True
         if accumulate not in (None, 'double', 'kahan'):
             raise ValueError(
                 'The argument "accumulate" must be None, "double" or'
@@ -886,7 +884,6 @@ class SimulationCUDA(object):
             self._model_version, self._precision, self._native_math, mode,
             two_d, block, minb, self._fp32_math, self._accumulate,
             stage, row_pad, lazy, self._sync_mode(), self._split_mode(),
-            self._exp64,
             tuple(v.qname() for v in acc),
             tuple(v.qname() for v in self._fields.keys()),
             tuple(v.qname() for v in inter_log))
@@ -899,8 +896,7 @@ class SimulationCUDA(object):
                 min_blocks=minb, math=self._fp32_math,
                 accumulate=self._accumulate, accumulate_states=acc,
                 stage=stage, row_pad=row_pad, stage_lazy=lazy,
-                sync=self._sync_mode(), split=self._split_mode(),
-                exp64=self._exp64)
+                sync=self._sync_mode(), split=self._split_mode())
             if len(self._kernels) > 16:
                 self._kernels.clear()
             self._kernels[key] = k
