@@ -482,6 +482,7 @@ class TissueAdjoint(object):
         sim._upload(be)
         items = np.full(len(self.cells), sim._vm.index(), dtype=np.int32)
         cells = np.ascontiguousarray(self.cells, dtype=np.int64)
+        be.log_sig = None
         be.check(lib.mkg_set_log(h, _lib.i32ptr(items), _lib.i64ptr(cells),
                                  len(cells), 0))
         be.check(lib.mkg_set_tuning(h, 0, 0, 0))

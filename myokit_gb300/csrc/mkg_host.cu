@@ -112,6 +112,94 @@ __global__ void k_soa_to_aos(const Real *__restrict__ in, double *out,
     }
 }
 
+/* Tiled forms of the two conversions above, for nvar up to MKG_TILE_NVAR:
+ * a block moves tiles of MKG_TILE_CELLS cells, whose AoS rows are one
+ * contiguous run of nvar * MKG_TILE_CELLS doubles, through shared memory,
+ * so that the AoS side is read or written in full contiguous runs and the
+ * SoA side as MKG_TILE_CELLS consecutive cells per state. Same conversions,
+ * bit for bit; no division per element. */
+#define MKG_TILE_CELLS 32
+#define MKG_TILE_NVAR 96
+
+template <typename Real>
+__global__ void __launch_bounds__(256)
+k_aos_to_soa_tiled(const double *__restrict__ in, Real *out, long long ncell,
+                   int nvar, long long pitch, Slots sl, void *alt)
+{
+    __shared__ double tile[MKG_TILE_CELLS * MKG_TILE_NVAR];
+    const long long ntile = (ncell + MKG_TILE_CELLS - 1) / MKG_TILE_CELLS;
+    for (long long t = blockIdx.x; t < ntile; t += gridDim.x) {
+        const long long c0 = t * MKG_TILE_CELLS;
+        const int nc = (int)min((long long)MKG_TILE_CELLS, ncell - c0);
+        const int nv = nc * nvar;
+        const double *src = in + c0 * nvar;
+        for (int k = threadIdx.x; k < nv; k += blockDim.x) tile[k] = src[k];
+        __syncthreads();
+        for (int k = threadIdx.x; k < nvar * MKG_TILE_CELLS;
+             k += blockDim.x) {
+            const int s = k / MKG_TILE_CELLS;
+            const int cc = k - s * MKG_TILE_CELLS;
+            if (cc >= nc) continue;
+            const long long c = c0 + cc;
+            const double v = tile[cc * nvar + s];
+            const int j = sl.hi_slot ? sl.hi_slot[s] : -1;
+            if (j >= 0 && sl.hi_mode == MKG_HI_DOUBLE) {
+                if (s == sl.skip_var) ((double *)alt)[c] = v;
+                else ((double *)sl.hi)[(long long)j * pitch + c] = v;
+                continue;
+            }
+            const Real x = (Real)v;
+            if (s == sl.skip_var) {
+                if (sl.v_double) ((double *)alt)[c] = v;
+                else ((Real *)alt)[c] = x;
+            } else {
+                out[(long long)s * pitch + c] = x;
+            }
+            if (j >= 0 && sl.hi_mode == MKG_HI_KAHAN)
+                ((Real *)sl.hi)[(long long)j * pitch + c] =
+                    (Real)((double)x - v);
+        }
+        __syncthreads();
+    }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(256)
+k_soa_to_aos_tiled(const Real *__restrict__ in, double *out, long long ncell,
+                   int nvar, long long pitch, Slots sl, const void *alt)
+{
+    __shared__ double tile[MKG_TILE_CELLS * MKG_TILE_NVAR];
+    const long long ntile = (ncell + MKG_TILE_CELLS - 1) / MKG_TILE_CELLS;
+    for (long long t = blockIdx.x; t < ntile; t += gridDim.x) {
+        const long long c0 = t * MKG_TILE_CELLS;
+        const int nc = (int)min((long long)MKG_TILE_CELLS, ncell - c0);
+        for (int k = threadIdx.x; k < nvar * MKG_TILE_CELLS;
+             k += blockDim.x) {
+            const int s = k / MKG_TILE_CELLS;
+            const int cc = k - s * MKG_TILE_CELLS;
+            if (cc >= nc) continue;
+            const long long c = c0 + cc;
+            const int j = sl.hi_slot ? sl.hi_slot[s] : -1;
+            double v;
+            if (s == sl.skip_var)
+                v = sl.v_double ? ((const double *)alt)[c]
+                                : (double)((const Real *)alt)[c];
+            else if (j >= 0 && sl.hi_mode == MKG_HI_DOUBLE)
+                v = ((const double *)sl.hi)[(long long)j * pitch + c];
+            else
+                v = (double)in[(long long)s * pitch + c];
+            if (j >= 0 && sl.hi_mode == MKG_HI_KAHAN)
+                v -= (double)((const Real *)sl.hi)[(long long)j * pitch + c];
+            tile[cc * nvar + s] = v;
+        }
+        __syncthreads();
+        const int nv = nc * nvar;
+        double *dst = out + c0 * nvar;
+        for (int k = threadIdx.x; k < nv; k += blockDim.x) dst[k] = tile[k];
+        __syncthreads();
+    }
+}
+
 template <typename Real>
 __global__ void k_convert(const double *__restrict__ in, Real *out,
                           long long n)
@@ -423,6 +511,15 @@ Slots plain_slots()
     return sl;
 }
 
+/* Blocks for the tiled conversions: one tile of MKG_TILE_CELLS cells per
+ * block and pass, at most 8 resident 256-thread blocks per SM */
+int tile_grid(const mkg_sim *s)
+{
+    const long long tiles = (s->ncell + MKG_TILE_CELLS - 1) / MKG_TILE_CELLS;
+    const long long cap = 8LL * std::max(s->num_sms, 1);
+    return (int)std::max<long long>(1, std::min(tiles, cap));
+}
+
 template <typename Real>
 int upload_soa(mkg_sim *s, const double *aos, int nvar, void *dst, Slots sl,
                void *alt)
@@ -433,8 +530,13 @@ int upload_soa(mkg_sim *s, const double *aos, int nvar, void *dst, Slots sl,
     CK(s, cudaMemcpyAsync(s->d_stage, aos, bytes, cudaMemcpyHostToDevice,
                           s->stream));
     s->n_launches++;
-    k_aos_to_soa<Real><<<grid_for(s->ncell * nvar), 256, 0, s->stream>>>(
-        s->d_stage, (Real *)dst, s->ncell, nvar, s->pitch, sl, alt);
+    if (nvar <= MKG_TILE_NVAR)
+        k_aos_to_soa_tiled<Real><<<tile_grid(s), 256, 0, s->stream>>>(
+            s->d_stage, (Real *)dst, s->ncell, nvar, s->pitch, sl, alt);
+    else
+        k_aos_to_soa<Real><<<grid_for(s->ncell * nvar), 256, 0,
+                             s->stream>>>(
+            s->d_stage, (Real *)dst, s->ncell, nvar, s->pitch, sl, alt);
     CK(s, cudaGetLastError());
     CK(s, cudaStreamSynchronize(s->stream));
     return MKG_OK;
@@ -448,8 +550,15 @@ int download_soa(mkg_sim *s, double *aos, int nvar, const void *src,
     int r = ensure_stage(s, bytes);
     if (r) return r;
     s->n_launches++;
-    k_soa_to_aos<Real><<<grid_for(s->ncell * nvar), 256, 0, s->stream>>>(
-        (const Real *)src, s->d_stage, s->ncell, nvar, s->pitch, sl, alt);
+    if (nvar <= MKG_TILE_NVAR)
+        k_soa_to_aos_tiled<Real><<<tile_grid(s), 256, 0, s->stream>>>(
+            (const Real *)src, s->d_stage, s->ncell, nvar, s->pitch, sl,
+            alt);
+    else
+        k_soa_to_aos<Real><<<grid_for(s->ncell * nvar), 256, 0,
+                             s->stream>>>(
+            (const Real *)src, s->d_stage, s->ncell, nvar, s->pitch, sl,
+            alt);
     CK(s, cudaGetLastError());
     CK(s, cudaMemcpyAsync(aos, s->d_stage, bytes, cudaMemcpyDeviceToHost,
                           s->stream));

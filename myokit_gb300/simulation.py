@@ -77,6 +77,10 @@ class _Backend(object):
             _lib.ctypes.byref(handle)))
         self.h = handle
         self.cfg = cfg
+        # What the handle's log columns were last set to by run_frames
+        # (None after any other setting): the frame columns of a large
+        # grid are then not rebuilt and uploaded again for the next call
+        self.log_sig = None
 
     def check(self, code):
         return _lib.check(code, self.h)
@@ -1162,6 +1166,7 @@ class SimulationCUDA(object):
         items = np.ascontiguousarray([c[0] for c in cols], dtype=np.int32)
         cells = np.ascontiguousarray([c[1] for c in cols], dtype=np.int64)
         logging_states = any(c[0] < self._nstate for c in cols)
+        be.log_sig = None
         be.check(lib.mkg_set_log(
             h, _lib.i32ptr(items), _lib.i64ptr(cells), len(cols),
             1 if logging_states else 0))
@@ -1295,10 +1300,14 @@ class SimulationCUDA(object):
             n0 = _lib.ctypes.c_int64()
             lib.mkg_launch_count(h, _lib.ctypes.byref(n0))
             self._upload(be)
-            items = np.full(self._ntotal, var.index(), dtype=np.int32)
-            cells = np.arange(self._ntotal, dtype=np.int64)
-            be.check(lib.mkg_set_log(h, _lib.i32ptr(items),
-                                     _lib.i64ptr(cells), len(cells), 0))
+            sig = ('frames', var.index())
+            if be.log_sig != sig:
+                items = np.full(self._ntotal, var.index(), dtype=np.int32)
+                cells = np.arange(self._ntotal, dtype=np.int64)
+                be.log_sig = None
+                be.check(lib.mkg_set_log(h, _lib.i32ptr(items),
+                                         _lib.i64ptr(cells), len(cells), 0))
+                be.log_sig = sig
             be.check(lib.mkg_set_tuning(h, self._launch_steps(),
                                         self._blocks_per_sm, self._graphs))
             torch.cuda.synchronize(self._device)

@@ -379,3 +379,25 @@ def test_run_frames_equal_logged_values(decker):
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
     assert np.array_equal(out[0][2], out[1][2])
+
+
+def test_run_frames_after_probe_runs(decker):
+    # Frame runs keep their log columns between calls; a probe-logged run
+    # in between replaces them, and the next frame run sets them again
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    out = []
+    for mixed in (False, True):
+        s = mg.SimulationCUDA(decker, p, ncells=(40, 24), rl=True)
+        s.set_paced_cells(3, 24)
+        frames = []
+        for i in range(3):
+            if mixed and i == 1:
+                st, t0 = s.state_array(), s.time()
+                s.run(1.5, log=['engine.time', '3.3.membrane.V'],
+                      log_interval=0.5)
+                s.set_state(st)
+                s.set_time(t0)
+            t, f = s.run_frames(1.5, 0.5)
+            frames.append(f.cpu().numpy())
+        out.append(np.concatenate(frames))
+    assert np.array_equal(out[0], out[1])
