@@ -116,11 +116,12 @@ def test_frames_to_block(br77):
 BATCH_FIELDS = ['ina.Gbar', 'ikr.Gbar', 'ik1.Gbar']
 
 
-def _oracle_1d(model, ncell, conns, paced, fields, dt, duration, log):
+def _oracle_1d(model, ncell, conns, paced, fields, dt, duration, log,
+               protocol=None):
     from oracle.refsim import ReferenceCpuSimulation
     import os
-    s = ReferenceCpuSimulation(model, _p(), ncells=ncell, precision=DP,
-                               rl=True)
+    s = ReferenceCpuSimulation(model, protocol or _p(), ncells=ncell,
+                               precision=DP, rl=True)
     s.set_threads(os.cpu_count() or 1)
     s.set_step_size(dt)
     s.set_connections(conns)
@@ -241,3 +242,53 @@ def test_reference_cable_chains_equal_conductance_field(decker):
     for k in log:
         assert np.array_equal(np.asarray(d[k]), np.asarray(ref[k])), k
     assert np.array_equal(np.asarray(s.state()).reshape(n, -1), st_ref)
+
+
+_CONFIG_REF = {}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('mode', ['fp64', 'fp32+kahan'])
+def test_batched_cables_configuration_vs_reference(decker, mode):
+    # The benchmark's batch at its own size: 512 cables of 50-2000 cells
+    # (5.2e5 cells, seed 3), six conductances per cable, the first 5 cells
+    # of each paced, dt 0.01 ms, over 2 ms (200 steps, the paced upstroke
+    # included), against one 1D oracle simulation with connection chains
+    # (computed once for both modes)
+    import bench
+    rng = np.random.default_rng(3)
+    lengths = rng.integers(50, 2001, 512)
+    fields = {name: decker.get(name).eval() * rng.lognormal(0, 0.3, 512)
+              for name in bench.CABLE_FIELDS}
+    starts = np.concatenate([[0], np.cumsum(lengths)[:-1]])
+    n = int(lengths.sum())
+    conns = [(int(a + k), int(a + k + 1), 10.0)
+             for a, ln in zip(starts, lengths) for k in range(int(ln) - 1)]
+    paced = [int(a + k) for a in starts for k in range(5)]
+    per_cell = {name: np.repeat(v, lengths) for name, v in fields.items()}
+    cells = sorted(set([0, n - 1] + [int(a + k) for a in starts[::37]
+                                      for k in (0, 4, 5, 40)]))
+    log = ['engine.time'] + ['%d.membrane.V' % c for c in cells]
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    if 'ref' not in _CONFIG_REF:
+        _CONFIG_REF['ref'] = _oracle_1d(decker, n, conns, paced, per_cell,
+                                        0.01, 2, log, p)
+    ref, st_ref = _CONFIG_REF['ref']
+    kw = {'precision': DP} if mode == 'fp64' else {
+        'precision': SP, 'accumulate': 'kahan'}
+    b = CableBatch(decker, lengths, p, conductance=10.0, paced_cells=5,
+                   fields=fields, rl=True, steps_per_launch=100, **kw)
+    b.sim.set_step_size(0.01)
+    d = b.sim.run(2, log=log, log_interval=0.5)
+    dv = max(float(np.max(np.abs(np.asarray(d[k], dtype=float) -
+                                 np.asarray(ref[k])))) for k in log[1:])
+    st = b.sim.state_array().reshape(n, -1)
+    i_vm = decker.label('membrane_potential').index()
+    fv = float(np.max(np.abs(st[:, i_vm] - st_ref[:, i_vm])))
+    assert max(np.asarray(ref[k]).max() for k in log[1:]) > 0
+    if mode == 'fp64':
+        assert dv <= 1e-9 and fv <= 1e-9
+        scale = np.max(np.abs(st_ref), axis=0) + 1e-300
+        assert np.max(np.abs(st - st_ref) / scale) <= 1e-9
+    else:
+        assert dv <= 0.5 and fv <= 0.5
