@@ -118,3 +118,48 @@ def test_schedule_pacing_errors():
         # Two events starting at the same time
         _lib.schedule_preview([[1, 0, 1, 0, 0], [1, 0, 2, 0, 0]], 0, 1, 0.1,
                               1, 100)
+
+
+def _decays(n_state):
+    # A model of n_state independent decays, V among them (for diffusion)
+    m = myokit.Model('decays')
+    c = m.add_component('c')
+    t = c.add_variable('t')
+    t.set_binding('time')
+    t.set_rhs(0)
+    for i in range(n_state):
+        x = c.add_variable('x%d' % i)
+        x.promote(float(i + 1))
+        x.set_rhs('-%g * x%d' % (0.01 * (i + 1), i))
+    c.get('x0').set_label('membrane_potential')
+    idiff = c.add_variable('idiff')
+    idiff.set_rhs(0)
+    idiff.set_binding('diffusion_current')
+    m.validate()
+    return m
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('n_state', [5, 96, 97, 130])
+@pytest.mark.parametrize('precision', ['single', 'double'])
+def test_state_round_trip_through_device_layout(n_state, precision):
+    # The state goes to the device's plane layout and back: exact in
+    # double precision, float rounding in single precision, for models
+    # within the tiled conversion's limit (96 states) and beyond it, on a
+    # cell count that is not a multiple of the 32-cell tile
+    import myokit_gb300 as mg
+    prec = myokit.DOUBLE_PRECISION if precision == 'double' else \
+        myokit.SINGLE_PRECISION
+    s = mg.SimulationCUDA(_decays(n_state), ncells=(37, 23), precision=prec)
+    s.run(0.01)
+    be = s._backend[1]
+    n = s._nstate * s._ntotal
+    rng = np.random.default_rng(n_state)
+    for _ in range(2):
+        x = np.ascontiguousarray(rng.normal(size=n) * 30)
+        be.check(be.lib.mkg_set_state(be.h, _lib.dptr(x), n))
+        y = np.empty(n)
+        be.check(be.lib.mkg_get_state(be.h, _lib.dptr(y), n))
+        want = x if precision == 'double' else \
+            x.astype(np.float32).astype(float)
+        assert np.array_equal(y, want)
