@@ -137,3 +137,27 @@ def test_split_nan_halt():
     with pytest.raises(myokit.SimulationError, match='Time:  1.23'):
         s.run(5)
     assert s._last_kernel.split == 4
+
+
+@pytest.mark.gpu
+def test_adjoint_of_a_split_simulation(br77):
+    # The adjoint's trajectory kernel is never split; on a handle made for
+    # a split kernel it gets the same gradients as on an unsplit one
+    from myokit_gb300 import adjoint
+    out = []
+    for split in (1, 4):
+        p = myokit.pacing.blocktrain(period=1000, duration=2, offset=1)
+        s = mg.SimulationCUDA(br77, p, ncells=100, precision=DP, block=128)
+        s._split = split
+        s.set_paced_cells(3)
+        s.set_field('isi.gsBar', np.linspace(0.07, 0.11, 100))
+        s.run(0.5)
+        assert s._last_kernel.split == split
+        adj = adjoint.TissueAdjoint(s, [0, 40, 99], segment_steps=50)
+        target = np.zeros((24, 3)) - 80
+        out.append(adj.loss_and_gradient(12, target, 0.5))
+    (L1, g1), (L4, g4) = out
+    assert abs(L4 - L1) <= 1e-12 * abs(L1)
+    np.testing.assert_allclose(g4['isi.gsBar'], g1['isi.gsBar'],
+                               rtol=1e-9, atol=1e-12 * abs(L1))
+    assert abs(g4['gx'] - g1['gx']) <= 1e-9 * abs(g1['gx'])
