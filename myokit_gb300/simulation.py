@@ -228,6 +228,7 @@ class SimulationCUDA(object):
             self.set_conductance()
         self._gx_field = None
         self._gy_field = None
+        self._g_arrays = None      # (key, gx, gy) arrays of the above
         self._connections = None
         self._paced_cells = None
         if self._diffusion_enabled:
@@ -1120,10 +1121,15 @@ class SimulationCUDA(object):
             be.check(lib.mkg_set_conductance(
                 h, self._gx or 0.0, self._gy or 0.0))
         elif mode == _exp.DIFF_HETERO:
-            gx = np.ascontiguousarray(self._gx_field, dtype=float)
-            gy = np.ascontiguousarray(
-                self._gy_field if self._gy_field is not None else [],
-                dtype=float)
+            # Converted once per set_conductance_field (the fields are
+            # lists, as the reference keeps them)
+            key = (id(self._gx_field), id(self._gy_field))
+            if self._g_arrays is None or self._g_arrays[0] != key:
+                self._g_arrays = (key, np.ascontiguousarray(
+                    self._gx_field, dtype=float), np.ascontiguousarray(
+                    self._gy_field if self._gy_field is not None else [],
+                    dtype=float))
+            gx, gy = self._g_arrays[1:]
             be.check(lib.mkg_set_conductance_field(
                 h, _lib.dptr(gx), gx.size, _lib.dptr(gy), gy.size))
         elif mode == _exp.DIFF_CONN:
