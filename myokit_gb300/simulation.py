@@ -348,6 +348,7 @@ class SimulationCUDA(object):
             raise ValueError('Invalid conductance gy=' + str(gy))
         self._gx, self._gy = gx, gy
         self._gx_field = self._gy_field = None
+        self._g_arrays = None
         self._connections = None
 
     def set_conductance_field(self, gx, gy=None):
@@ -385,6 +386,7 @@ class SimulationCUDA(object):
         if (gy is not None) and np.any(gy < 0):
             raise ValueError(
                 'The argument `gy` can not contain negative values.')
+        self._g_arrays = None
         self._gx_field = list(gx.reshape((self._nx - 1) * self._ny))
         if gy is None:
             self._gy_field = None
@@ -430,6 +432,7 @@ class SimulationCUDA(object):
             conns.append((i, j, c))
         self._connections = conns
         self._gx_field = self._gy_field = None
+        self._g_arrays = None
 
     def neighbors(self, x, y=None):
         """
