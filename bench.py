@@ -100,6 +100,9 @@ def parse():
                         ' 300 ms, the 2048x2048 S1-S2 protocol for 1000 ms')
     p.add_argument('--profile', action='store_true',
                    help='run one small sheet case for a profiler and exit')
+    p.add_argument('--tune-only', default='',
+                   help='with --tune: a comma list of the configurations'
+                        ' to tune (sheet512-fp32, cable200-fp64, ...)')
     p.add_argument('--tune', action='store_true',
                    help='autotune the launch shape of every benchmark'
                         ' configuration, print the timings and the table'
@@ -978,9 +981,10 @@ def _cables(m, p, **kw):
 
 def tune_configs(args):
     """
-    Runs the autotuner on each benchmark configuration: the 512 x 512 sheet
-    in every precision mode, the 2048 x 2048 sheet (FP32 and Kahan), the
-    512 batched cables and the 200-cell cable. Results go to the user cache
+    Runs the autotuner on each benchmark configuration (or those
+    --tune-only names): the 512 x 512 sheet in every precision mode, the
+    2048 x 2048 sheet (FP32 and Kahan), the 512 batched cables, the 200-cell
+    cable and the 2048-cell FP64 cable. Results go to the user cache
     (MYOKIT_GB300_CACHE or ~/.cache/myokit_gb300); the table is printed.
     """
     from myokit_gb300._deps import myokit
@@ -988,7 +992,11 @@ def tune_configs(args):
     from myokit_gb300 import autotune as at
     SP, DP = myokit.SINGLE_PRECISION, myokit.DOUBLE_PRECISION
 
+    only = set(filter(None, (args.tune_only or '').split(',')))
+
     def tune(name, s):
+        if only and name not in only:
+            return
         t0 = time.time()
         best, res = at.autotune(s)
         print(json.dumps({'config': name, 'best': str(best), 'seconds':
@@ -1016,12 +1024,15 @@ def tune_configs(args):
         os.path.dirname(myokit.__file__), 'tests', 'data',
         'beeler-1977-model.mmt'))
     for label, prec, kw in (('fp64', DP, {}),
-                            ('kahan', SP, {'accumulate': 'kahan'})):
+                            ('kahan', SP, {'accumulate': 'kahan'}),
+                            ('fp32', SP, {})):
         s = mg.SimulationCUDA(br, p, ncells=200, precision=prec, **kw)
         s.set_step_size(0.005)
         s.set_conductance(9)
         s.set_paced_cells(5)
         tune('cable200-' + label, s)
+    # The FP64 reference of the S1 phase: a row of the 2048 x 2048 sheet
+    tune('cable2048-fp64', make_s1_cable(mg.SimulationCUDA, DP, 2048))
     with open(at._cache_path()) as f:
         print(f.read())
     return 0

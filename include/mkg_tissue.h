@@ -91,9 +91,11 @@ typedef struct mkg_config {
                                per CTA is warps x stage x bytes + 128 */
     int32_t v_double;       /* 1: V is stored and updated in FP64 (hi_mode 1
                                with V among the selected states) */
-    int32_t split;          /* warps per warp tile (1, 2 or 4): the kernel
-                               divides each tile's state updates among that
-                               many warps of one CTA (0 is taken as 1) */
+    int32_t split;          /* warps per warp tile (1, 2, 4, 8 or 16): the
+                               kernel divides each tile's state updates
+                               among that many warps, of one CTA or, when
+                               more than the CTA holds, of a cluster of
+                               whole CTAs (at most 8; 0 is taken as 1) */
 } mkg_config;
 
 /*

@@ -44,12 +44,15 @@ _CANDIDATES = [
 _CANDIDATES_FP64 = [((128, 1), 1, 0, False, _B), ((256, 1), 1, 0, False, _B),
                     ((64, 1), 1, 0, False, _B), ((32, 1), 1, 0, False, _B),
                     ((256, 1), 1, 0, True, _B), ((256, 1), 1, 0, False, _N)]
-# Grids with fewer warp tiles than SMs: teams of 2 or 4 warps share each
-# tile's work (a sixth entry: warps per tile), one team per CTA or two
+# Grids with fewer warp tiles than SMs: teams of 2 to 16 warps share each
+# tile's work (a sixth entry: warps per tile): one team per CTA or two, or
+# one team per cluster of 2 or 4 CTAs
 _CANDIDATES_SPLIT = [((64, 1), 1, 0, False, _B, 2),
                      ((128, 1), 1, 0, False, _B, 4),
                      ((128, 1), 1, 0, False, _B, 2),
-                     ((256, 1), 1, 0, False, _B, 4)]
+                     ((256, 1), 1, 0, False, _B, 4),
+                     ((128, 1), 1, 0, False, _B, 8),
+                     ((128, 1), 1, 0, False, _B, 16)]
 
 
 def _cache_path():

@@ -745,6 +745,13 @@ int encode_stage_maps(mkg_sim *s)
     return MKG_OK;
 }
 
+/* CTAs per cluster: a split team larger than the CTA is a cluster */
+int cluster_ctas(const mkg_sim *s)
+{
+    const int nwarp = s->cfg.block_x / 32;
+    return s->cfg.split > nwarp ? s->cfg.split / nwarp : 1;
+}
+
 /* CTAs needed to give every warp tile a warp (a team of cfg.split warps
  * when the kernel divides each tile's work) */
 long long blocks_needed(const mkg_sim *s, const mkg_launch *a)
@@ -904,15 +911,25 @@ int mkg_create(const mkg_config *cfg, const void *cubin, size_t cubin_size,
         return set_err(nullptr, MKG_ERR_ARG, "v_double needs hi_mode 1");
     if (cfg->stage < 0 || cfg->stage > 2)
         return set_err(nullptr, MKG_ERR_ARG, "stage must be 0, 1 or 2");
-    if (cfg->split < 0 || cfg->split > 4 || cfg->split == 3)
-        return set_err(nullptr, MKG_ERR_ARG, "split must be 1, 2 or 4");
-    if (cfg->split > 1 &&
-        ((cfg->block_x / 32) % cfg->split != 0 ||
-         cfg->block_x / 32 / cfg->split > 15 || cfg->stage ||
-         cfg->hi_mode != MKG_HI_NONE))
+    if (cfg->split < 0 || cfg->split > 16 ||
+        (cfg->split > 1 && (cfg->split & (cfg->split - 1))))
         return set_err(nullptr, MKG_ERR_ARG,
-                       "a split kernel needs whole teams of at most 15 per"
-                       " CTA, no staging and no accumulation planes");
+                       "split must be 1, 2, 4, 8 or 16");
+    if (cfg->split > 1) {
+        const int nwarp = cfg->block_x / 32;
+        const bool cta_team = cfg->split <= nwarp &&
+                              nwarp % cfg->split == 0 &&
+                              nwarp / cfg->split <= 15;
+        const bool cluster_team = cfg->split > nwarp &&
+                                  cfg->split % nwarp == 0 &&
+                                  cfg->split / nwarp <= 8;
+        if ((!cta_team && !cluster_team) || cfg->stage ||
+            cfg->hi_mode != MKG_HI_NONE)
+            return set_err(nullptr, MKG_ERR_ARG,
+                           "a split kernel needs whole teams of at most 15"
+                           " per CTA, or teams of 2 to 8 whole CTAs, no"
+                           " staging and no accumulation planes");
+    }
     if (cfg->stage) {
         /* Tensor copy limits: 256 planes per box, int32 coordinates */
         StageLayout L;
@@ -1438,6 +1455,9 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
                                     : s->occ_blocks;
     long long coop_blocks = std::min<long long>(nblocks,
                                                 (long long)bpsm * s->num_sms);
+    /* Split teams larger than the CTA are clusters of whole CTAs */
+    const int ncl = cluster_ctas(s);
+    coop_blocks -= coop_blocks % ncl;
     int spl = s->steps_per_launch > 0 ? s->steps_per_launch : 1 << 20;
 
     /* All launches of the chunk are queued without host synchronisation;
@@ -1486,19 +1506,25 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
             void *args_p[] = {&a, &b, &s->junction};
             cudaLaunchConfig_t lc;
             memset(&lc, 0, sizeof(lc));
-            cudaLaunchAttribute attr[1];
+            cudaLaunchAttribute attr[2];
             lc.blockDim = dim3(threads, 1, 1);
             lc.stream = s->stream;
+            lc.attrs = attr;
             long long grid;
             if (m > 1) {
                 grid = coop_blocks;
-                attr[0].id = cudaLaunchAttributeCooperative;
-                attr[0].val.cooperative = 1;
-                lc.attrs = attr;
-                lc.numAttrs = 1;
+                attr[lc.numAttrs].id = cudaLaunchAttributeCooperative;
+                attr[lc.numAttrs++].val.cooperative = 1;
                 epoch += (int)(m - 1);
             } else {
                 grid = std::min<long long>(nblocks, 1 << 30);
+                grid -= grid % ncl;
+            }
+            if (ncl > 1) {
+                attr[lc.numAttrs].id = cudaLaunchAttributeClusterDimension;
+                attr[lc.numAttrs].val.clusterDim.x = (unsigned)ncl;
+                attr[lc.numAttrs].val.clusterDim.y = 1;
+                attr[lc.numAttrs++].val.clusterDim.z = 1;
             }
             lc.gridDim = dim3((unsigned)grid, 1, 1);
             lc.dynamicSmemBytes = s->tile_smem;
@@ -1535,6 +1561,12 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
     CK(s, cudaMemcpyAsync(s->h_status, s->d_status, sizeof(mkg_status),
                           cudaMemcpyDeviceToHost, s->stream));
     CK(s, cudaStreamSynchronize(s->stream));
+    if (s->h_status->error == MKG_DEV_LAUNCH) {
+        s->running = false;
+        return set_err(s, MKG_ERR_CUDA,
+                       "the kernel was launched with clusters of another"
+                       " size than it was generated for");
+    }
     if (s->h_status->error != MKG_DEV_OK) {
         s->running = false;
         return set_err(s, MKG_ERR_TIMEOUT,
@@ -1659,10 +1691,12 @@ int mkg_set_partner(mkg_sim *s, mkg_sim *partner, double gft, int64_t cty)
                        " precision on the same device");
     if (c.diffusion != MKG_DIFF_GRID || d.diffusion != MKG_DIFF_GRID ||
         !c.two_d || !d.two_d || c.stage || d.stage ||
-        c.hi_mode != MKG_HI_NONE || d.hi_mode != MKG_HI_NONE)
+        c.hi_mode != MKG_HI_NONE || d.hi_mode != MKG_HI_NONE ||
+        c.split > 1 || d.split > 1)
         return set_err(s, MKG_ERR_ARG,
                        "fiber-tissue simulations use 2D grid diffusion"
-                       " without staging or accumulation modes");
+                       " without staging, accumulation modes or split"
+                       " tiles");
     if (c.ny > d.ny || cty < 0 || cty + c.ny > d.ny)
         return set_err(s, MKG_ERR_ARG,
                        "the junction rows must lie inside the tissue");

@@ -13,6 +13,8 @@
 #define MKG_DEV_TIMEOUT   1   /* grid barrier wait exceeded timeout_ns */
 #define MKG_DEV_STAGE     2   /* tile staging: the host's layout differs from
                                  the kernel's, or a copy wait timed out */
+#define MKG_DEV_LAUNCH    3   /* the launch's cluster shape differs from the
+                                 kernel's */
 
 #define MKG_NO_HALT 0x7fffffff
 

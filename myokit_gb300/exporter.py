@@ -512,20 +512,30 @@ class TissueKernel(object):
         self.v_double = (self.accumulate == 'double' and
                          self.i_vm in self.hi_index)
         self.traj = bool(traj)
-        # Warps per warp tile (1, 2 or 4). Split teams read their states
-        # themselves and meet at a named CTA barrier, so they take none of
-        # tile staging, accumulation planes, trajectory output or
-        # neighbour synchronisation; where one of those is asked for, or
-        # the CTA does not hold whole teams (at most 15 per CTA: named
-        # barriers 1-15), the kernel is not split.
+        # Warps per warp tile (1, 2, 4, 8 or 16). Split teams read their
+        # states themselves and meet at a team barrier, so they take none
+        # of tile staging, accumulation planes, trajectory output or
+        # neighbour synchronisation; where one of those is asked for the
+        # kernel is not split. A team is either part of one CTA (at most
+        # 15 teams per CTA: named barriers 1-15) or a cluster of 2 to 8
+        # whole CTAs (split_cl CTAs: a team larger than the CTA); other
+        # shapes are not split either.
         self.split = int(split)
-        if self.split not in (1, 2, 4):
-            raise ValueError('split must be 1, 2 or 4')
+        if self.split not in (1, 2, 4, 8, 16):
+            raise ValueError('split must be 1, 2, 4, 8 or 16')
         nwarp = self.block[0] // 32
         if self.split > 1 and (
-                self.accumulate or self.traj or self.block[1] != 1
-                or nwarp % self.split or nwarp // self.split > 15):
+                self.accumulate or self.traj or self.block[1] != 1):
             self.split = 1
+        if self.split > nwarp:
+            if self.split % nwarp or self.split // nwarp > 8:
+                self.split = 1
+        elif self.split > 1 and (nwarp % self.split or
+                                 nwarp // self.split > 15):
+            self.split = 1
+        self.split_cl = max(1, self.split // nwarp)
+        self.split_nslot = 0
+        self.split_terms = {}
         if self.split > 1:
             stage = False
             sync = 'barrier'
@@ -706,6 +716,9 @@ class TissueKernel(object):
         loads = []
         updates = []
         state_src = []       # (name, value at t) per state, plain loads
+        # (target, new value) of each plain update, for split kernels,
+        # which write the states after the team has read them
+        self._upd_expr = {}
         hiD = '((double *)hi)'
         hiR = '((Real *)hi)'
         for i, s in enumerate(self.states):
@@ -745,6 +758,7 @@ class TissueKernel(object):
                 expf = w._fn('exp')
                 upd = f'{inf} - ({inf} - {n}) * {expf}(-dt_ / {tau})'
                 text = f'{tab}{target} = {upd};'
+                self._upd_expr[i] = (target, upd)
                 self.census.arith += 4
                 self.census.trans += 1
             else:
@@ -753,6 +767,7 @@ class TissueKernel(object):
                 self.census.arith += 2
                 if j is None:
                     text = f'{tab}{target} = {n} + dt_ * {d};'
+                    self._upd_expr[i] = (target, f'{n} + dt_ * {d}')
                 elif self.accumulate == 'double':
                     cur = 'V_' if i == self.i_vm else f'X{n}'
                     dst = target if i == self.i_vm else f'{hiD}[{hplane}]'
@@ -860,6 +875,8 @@ class TissueKernel(object):
 
         subs = {
             '@SPLIT@': str(self.split),
+            '@SPLIT_CL@': str(self.split_cl),
+            '@SPLIT_NSLOT@': str(self.split_nslot),
             '@SPLIT_BODY@': split_body,
             '@REAL@': real,
             '@VREAL@': 'double' if self.v_double else real,
@@ -917,19 +934,67 @@ class TissueKernel(object):
             '// Generated by myokit_gb300.exporter for model '
             + str(m.name()) + '\n' + abi + '\n' + text)
 
+    def _split_terms(self, rhs_of):
+        """
+        Additive decomposition of an expression into (coefficient, term)
+        pairs: through sums, differences, negation, multiplication and
+        division by literals, and references to intermediary variables
+        whose own right-hand sides decompose (cubic roots excluded, their
+        refinement needs the whole expression).
+        """
+        def terms(e, c):
+            if isinstance(e, myokit.PrefixPlus):
+                return terms(e[0], c)
+            if isinstance(e, myokit.PrefixMinus):
+                return terms(e[0], -c)
+            if isinstance(e, myokit.Plus):
+                return terms(e[0], c) + terms(e[1], c)
+            if isinstance(e, myokit.Minus):
+                return terms(e[0], c) + terms(e[1], -c)
+            if isinstance(e, myokit.Multiply):
+                for i in (0, 1):
+                    if isinstance(e[i], myokit.Number):
+                        return terms(e[1 - i], c * float(e[i].eval()))
+            if isinstance(e, myokit.Divide) and \
+                    isinstance(e[1], myokit.Number):
+                den = float(e[1].eval())
+                if den != 0:
+                    return terms(e[0], c / den)
+            if isinstance(e, myokit.Name):
+                n = self._name(e)
+                if n in rhs_of and n not in self.cubic:
+                    return terms(rhs_of[n], c)
+            return [(c, e)]
+        return terms
+
     def _split_body(self, items, updates, state_src, field_loads, log_a,
                     log_b):
         """
-        The per-warp code of a split tile: the state updates are divided
-        among the team's warps so that the largest share of work (each
-        update with every equation it needs, counted once per warp that
-        needs it) is small, by greedy assignment from the costliest update
-        down. Warp 0 also logs and checks the NaN halt, so it reads every
-        state and computes the logged intermediaries.
+        The per-warp code of a split tile. The work units are the updates
+        of the states, except that the derivative of a forward-Euler state
+        that no other equation uses is divided into its additive terms
+        (the currents of dV/dt, the alpha and beta terms of a gate), each a
+        unit of its own. Units are assigned greedily, from the costliest
+        down, to the warp whose share (every equation it needs, counted
+        once per warp that needs it) then stays smallest. A warp that holds
+        terms of another warp's state sums them and hands the partial sum
+        over in shared memory (distributed shared memory of the owner's
+        CTA when the team spans a cluster); the owner adds the partial sums
+        in a fixed order (the order of the warps), so results do not
+        depend on timing. Every warp reads the states it needs at t,
+        computes, and hands its partial sums over; the team then meets at
+        its barrier, and each warp writes its own states at t + dt. Warp 0
+        also logs and checks the NaN halt, so it reads every state and
+        computes the logged intermediaries.
         """
         P = self.split
+        nwarp = self.block[0] // 32
+        w = self.writer
         refs = {name: r for name, r, _, _ in items}
         cost = {name: c for name, _, _, c in items}
+        rhs_of = {self._name(lhs): rhs for lhs, rhs in self.rhs_eqs
+                  if isinstance(lhs, myokit.Name)}
+        terms = self._split_terms(rhs_of)
 
         def closure(roots):
             out = set()
@@ -942,49 +1007,115 @@ class TissueKernel(object):
                 todo.extend(refs[n])
             return out
 
-        # Update texts cost 2 (forward Euler) or an exp and 4 (Rush-Larsen)
-        upd = []
+        # Derivatives another equation (or the log) refers to are computed
+        # whole
+        used = set(self._inter_names)
+        for r in refs.values():
+            used |= r
+        dexpr = {self._name(lhs): rhs for lhs, rhs in self.rhs_eqs
+                 if isinstance(lhs, myokit.Derivative)}
+
+        # Units: (state, term index or None, needed equations, own cost)
+        units = []
+        split_terms = {}     # state -> [(coefficient, term), ...]
         for i, need, text in updates:
-            own = 24 if self.states[i] in self.rl_states else 2
-            upd.append((i, need, text, closure(need), own))
+            s = self.states[i]
+            d = self._name(s.lhs())
+            tl = None
+            if s not in self.rl_states and d not in used and d in dexpr:
+                tl = terms(dexpr[d], 1.0)
+                if len(tl) < 2 or len(tl) > 256:
+                    tl = None
+            if tl is None:
+                own = 24 if s in self.rl_states else 2
+                units.append((i, None, closure(need), own))
+                continue
+            split_terms[i] = tl
+            for k, (c, e) in enumerate(tl):
+                cen = OpCensus()
+                cen.add(e)
+                r = set(self._name(x) for x in e.references())
+                units.append((i, k, closure(r), cen.cost() + 2))
+
         groups = [set() for _ in range(P)]
         owns = [0] * P
-        targets = [[] for _ in range(P)]
+        assign = [[] for _ in range(P)]     # units per warp
         groups[0] |= closure(self._inter_names)
 
         def gcost(g, extra=frozenset()):
             return sum(cost[n] for n in groups[g] | extra)
-        for i, need, text, cl, own in sorted(
-                upd, key=lambda u: -(sum(cost[n] for n in u[3]) + u[4])):
-            g = min(range(P), key=lambda g: (gcost(g, cl) + owns[g] + own,
+        for u in sorted(units,
+                        key=lambda u: -(sum(cost[n] for n in u[2]) + u[3])):
+            g = min(range(P), key=lambda g: (gcost(g, u[2]) + owns[g] + u[3],
                                              g))
-            groups[g] |= cl
-            owns[g] += own
-            targets[g].append(i)
+            groups[g] |= u[2]
+            owns[g] += u[3]
+            assign[g].append(u)
+
+        # Owner of each divided state: the warp holding its costliest term
+        holders = {i: [] for i in split_terms}
+        for g in range(P):
+            for i, k, _, own in assign[g]:
+                if k is not None and g not in holders[i]:
+                    holders[i].append(g)
+        owner = {}
+        for i in split_terms:
+            best = max((own, -g) for g in range(P)
+                       for j, k, _, own in assign[g] if j == i and k is not None)
+            owner[i] = -best[1]
+            holders[i].sort()
+            owns[owner[i]] += len(holders[i])
+        # Shared-memory slots: one per (state, warp other than the owner)
+        slot = {}
+        for i in sorted(split_terms):
+            for g in holders[i]:
+                if g != owner[i]:
+                    slot[(i, g)] = len(slot)
+        self.split_nslot = len(slot)
+        self.split_terms = {self.states[i].qname(): len(t)
+                            for i, t in split_terms.items()}
         self.split_costs = [gcost(g) + owns[g] for g in range(P)]
+
+        def coef_term(c, e, first, acc):
+            t = w.ex(e)
+            if c == 1.0:
+                return f'{acc} = {t};' if first else f'{acc} += {t};'
+            if c == -1.0:
+                return f'{acc} = -({t});' if first else f'{acc} -= {t};'
+            cc = w.ex(myokit.Number(c))
+            return (f'{acc} = {cc} * ({t});' if first
+                    else f'{acc} += {cc} * ({t});')
 
         tab = '            '
         out = []
         for p in range(P):
-            mine = set(targets[p])
+            whole = [i for i, k, _, _ in assign[p] if k is None]
+            mine_terms = {}
+            for i, k, _, _ in assign[p]:
+                if k is not None:
+                    mine_terms.setdefault(i, []).append(k)
+            owned = [i for i in split_terms if owner[i] == p]
             # States read: those the part's equations and updates use
-            read = set(self._name(self.states[i]) for i in mine)
+            read = set(self._name(self.states[i]) for i in whole + owned)
             for n in groups[p]:
                 read |= refs[n]
+            for i, ks in mine_terms.items():
+                for k in ks:
+                    read |= set(self._name(x)
+                                for x in split_terms[i][k][1].references())
             sts = [(n, src) for n, src in state_src
                    if p == 0 or n in read]
             out.append(f'{tab}{"if" if p == 0 else "else if"} (part_ == {p})'
                        ' {')
             for n, _ in sts:
                 out.append(f'{tab}    Real {n} = 0;')
+            for i in whole:
+                out.append(f'{tab}    Real n{i}_ = 0;')
+            for i in sorted(mine_terms):
+                out.append(f'{tab}    Real q{i}_ = 0;')
             out.append(f'{tab}    if (live) {{')
             for n, src in sts:
                 out.append(f'{tab}        {n} = {src};')
-            out.append(f'{tab}    }}')
-            out.append(f'{tab}    // every warp of the team has read the'
-                       ' states at t')
-            out.append(f'{tab}    mkg_team_sync();')
-            out.append(f'{tab}    if (live) {{')
             out.append(f'{tab}    const Real idiff_ = (Real)id_;')
             out.append(f'{tab}    (void)idiff_;')
             out.append(f'{tab}    const Real pace_ = mkg_cell_pace(a, ix, iy,'
@@ -995,22 +1126,61 @@ class TissueKernel(object):
                 out.append(log_a)
             defined = set()
             done = set()
+            pend = [(i, k) for i in sorted(mine_terms)
+                    for k in mine_terms[i]]
+            started = set()
 
             def flush():
-                for i, need, text, _, _ in upd:
-                    if i in mine and i not in done and need <= defined:
-                        out.append(text)
+                for i, need, text in updates:
+                    if i in whole and i not in done and need <= defined:
+                        out.append(f'{tab}    n{i}_ = '
+                                   f'{self._upd_expr[i][1]};')
                         done.add(i)
+                for ik in list(pend):
+                    i, k = ik
+                    c, e = split_terms[i][k]
+                    r = set(self._name(x) for x in e.references())
+                    if (r & set(refs)) <= defined:
+                        out.append(f'{tab}    ' + coef_term(
+                            c, e, i not in started, f'q{i}_'))
+                        started.add(i)
+                        pend.remove(ik)
             flush()
             for name, _, line, _ in items:
                 if name in groups[p]:
                     out.append(line)
                     defined.add(name)
                     flush()
-            if done != mine:   # pragma: no cover
+            if done != set(whole) or pend:   # pragma: no cover
                 raise ValueError('Could not order the state updates.')
             if p == 0:
                 out.append(log_b)
+            # Partial sums of other warps' states
+            for i in sorted(mine_terms):
+                if owner[i] == p:
+                    continue
+                s = slot[(i, p)]
+                r = owner[i] // nwarp
+                if P > nwarp and r != p // nwarp:
+                    out.append(f'{tab}    MKG_PP_PUT({s}, {r}, q{i}_);')
+                else:
+                    out.append(f'{tab}    MKG_PP_LOCAL({s}, q{i}_);')
+            out.append(f'{tab}    }}')
+            out.append(f'{tab}    // the team read its states at t and'
+                       ' handed its partial sums over')
+            out.append(f'{tab}    mkg_team_sync();')
+            out.append(f'{tab}    if (live) {{')
+            for i in whole:
+                out.append(f'{tab}        {self._upd_expr[i][0]} = n{i}_;')
+            for i in owned:
+                parts = [f'q{i}_' if g == p else f'MKG_PP_GET({slot[(i, g)]})'
+                         for g in holders[i]]
+                acc = parts[0]
+                for t in parts[1:]:
+                    acc = f'({acc} + {t})'
+                n = self._name(self.states[i])
+                out.append(f'{tab}        {self._upd_expr[i][0]} = '
+                           f'{n} + dt_ * {acc};')
             out.append(f'{tab}    }}')
             out.append(f'{tab}}}')
         return '\n'.join(out)
