@@ -1506,11 +1506,13 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
             void *args_p[] = {&a, &b, &s->junction};
             cudaLaunchConfig_t lc;
             memset(&lc, 0, sizeof(lc));
-            cudaLaunchAttribute attr[2];
+            cudaLaunchAttribute attr[1];
             lc.blockDim = dim3(threads, 1, 1);
             lc.stream = s->stream;
             lc.attrs = attr;
             long long grid;
+            /* (a kernel with split teams larger than the CTA has its
+             * cluster shape compiled in; grids are whole clusters) */
             if (m > 1) {
                 grid = coop_blocks;
                 attr[lc.numAttrs].id = cudaLaunchAttributeCooperative;
@@ -1519,12 +1521,6 @@ int mkg_run_chunk(mkg_sim *s, int64_t max_steps, double *t_out,
             } else {
                 grid = std::min<long long>(nblocks, 1 << 30);
                 grid -= grid % ncl;
-            }
-            if (ncl > 1) {
-                attr[lc.numAttrs].id = cudaLaunchAttributeClusterDimension;
-                attr[lc.numAttrs].val.clusterDim.x = (unsigned)ncl;
-                attr[lc.numAttrs].val.clusterDim.y = 1;
-                attr[lc.numAttrs++].val.clusterDim.z = 1;
             }
             lc.gridDim = dim3((unsigned)grid, 1, 1);
             lc.dynamicSmemBytes = s->tile_smem;
