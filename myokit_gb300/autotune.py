@@ -106,10 +106,23 @@ def _apply(sim, block, min_blocks, spl, lazy=False, sync='barrier',
     sim._graphs = 1
 
 
+def _sm_count(device):
+    """SMs of a CUDA device (152 on a GB300, taken when it cannot be
+    read)."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return int(torch.cuda.get_device_properties(
+                device).multi_processor_count)
+    except Exception:   # pragma: no cover
+        pass
+    return 152
+
+
 def _few_tiles(sim):
-    """True when the grid has fewer warp tiles than a GB300 has SMs."""
+    """True when the grid has fewer warp tiles than the device has SMs."""
     tiles = -(-sim._nx // 32) * sim._ny
-    return tiles < 152
+    return tiles < _sm_count(sim._device)
 
 
 def autotune(sim, duration=None, candidates=None, store=True,

@@ -536,6 +536,7 @@ class TissueKernel(object):
         self.split_cl = max(1, self.split // nwarp)
         self.split_nslot = 0
         self.split_terms = {}
+        self.split_term_exprs = {}
         if self.split > 1:
             stage = False
             sync = 'barrier'
@@ -1074,6 +1075,9 @@ class TissueKernel(object):
         self.split_nslot = len(slot)
         self.split_terms = {self.states[i].qname(): len(t)
                             for i, t in split_terms.items()}
+        # The (coefficient, term) lists themselves, per divided state
+        self.split_term_exprs = {self.states[i].qname(): list(t)
+                                 for i, t in split_terms.items()}
         self.split_costs = [gcost(g) + owns[g] for g in range(P)]
 
         def coef_term(c, e, first, acc):

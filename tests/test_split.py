@@ -201,3 +201,42 @@ def test_adjoint_of_a_split_simulation(br77):
         np.testing.assert_allclose(g4['isi.gsBar'], g1['isi.gsBar'],
                                    rtol=1e-9, atol=1e-12 * abs(L1))
         assert abs(g4['gx'] - g1['gx']) <= 1e-9 * abs(g1['gx'])
+
+
+@pytest.mark.parametrize('name,rl', [('beeler-1977-model.mmt', False),
+                                     ('decker-2009.mmt', True),
+                                     ('lr-1991.mmt', False)])
+def test_divided_derivatives_add_up(name, rl):
+    # The terms a split kernel spreads over its warps add up to the
+    # derivative they come from: evaluated in double precision at the
+    # model's initial state, sum(c_k * T_k) equals dx/dt to rounding
+    s = _cable(load(name), DP, 8, 128, rl=rl)
+    k = s._kernel([])
+    assert k.split_term_exprs
+    m = k.model     # the simulation's own copy, whose variables terms use
+    # Values of every variable at the initial state, with pacing on and
+    # no diffusion current, in solvable order
+    sub = {}
+    for v, x in zip(m.states(), m.initial_values(as_floats=True)):
+        sub[myokit.Name(v)] = myokit.Number(x)
+    for label, value in (('pace', 1.0), ('diffusion_current', 0.0),
+                         ('time', 0.0)):
+        v = m.binding(label)
+        if v is not None:
+            sub[myokit.Name(v)] = myokit.Number(value)
+    for group in m.solvable_order().values():
+        for eq in group.equations(const=None):
+            if eq.lhs.var() in [x.var() for x in sub] and \
+                    not isinstance(eq.lhs, myokit.Derivative):
+                continue
+            val = eq.rhs.eval(subst=sub)
+            sub[eq.lhs] = myokit.Number(val)
+    checked = 0
+    for qname, terms in k.split_term_exprs.items():
+        v = m.get(qname)
+        d = sub[myokit.Derivative(myokit.Name(v))].eval()
+        total = sum(c * e.eval(subst=sub) for c, e in terms)
+        assert total == pytest.approx(d, rel=1e-12, abs=1e-12 * (
+            1 + sum(abs(c * e.eval(subst=sub)) for c, e in terms))), qname
+        checked += 1
+    assert checked >= 1
