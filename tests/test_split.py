@@ -113,6 +113,27 @@ def test_split_cable200_matches_golden(br77, split, block):
     assert worst < 1e-9
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize('split', [4, 16])
+def test_split_graph_chunks_match_golden(br77, split):
+    # Launches of 100 steps replayed from CUDA graphs (cooperative cluster
+    # launches captured in a graph for 16 warps per tile)
+    g = np.load(os.path.join(GOLDEN, 'br77_cable200_sim1d.npz'))
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    s = mg.SimulationCUDA(br77, p, ncells=200, precision=DP, block=128,
+                          steps_per_launch=100)
+    s._split = split
+    s.set_step_size(0.005)
+    s.set_conductance(9)
+    s.set_paced_cells(5)
+    d = s.run(20, log=['engine.time', 'membrane.V'], log_interval=1).npview()
+    assert s._last_kernel.split == split
+    assert s.last_run_stats()['launches'] >= 40
+    worst = max(np.max(np.abs(d['membrane.V', c] - g['%d_membrane_V' % c]))
+                for c in range(200))
+    assert worst < 1e-9
+
+
 def _same(a, b, n_state, rtol, vtol):
     # States: relative to each state's largest magnitude over the cells
     # (gates and concentrations span many decades); logs: absolute (mV)
