@@ -899,9 +899,12 @@ def config_c1(args, device):
         wall = time.perf_counter() - t0
         st = s.last_run_stats()
         logs[name] = d
+        k = s._last_kernel
         out[name] = {'value': 200 * 200000 / (st['kernel_ms'] / 1000),
                      'e2e': 200 * 200000 / wall, 'unit': UNIT,
-                     'wall_s': wall}
+                     'wall_s': wall, 'block': list(k.block),
+                     'warps_per_tile': k.split,
+                     'ctas_per_cluster': k.split_cl}
     try:
         sa = setup(myokit.Simulation1d)
         t0 = time.perf_counter()
