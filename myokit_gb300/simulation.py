@@ -262,7 +262,7 @@ class SimulationCUDA(object):
         # Between steps: 'barrier' (grid-wide) or 'neighbors' (each warp
         # waits for the warps whose cells it reads); None: tuned or barrier
         self._sync = None
-        # Warps per warp tile (1, 2 or 4); None: tuned or 1
+        # Warps per warp tile (1, 2, 4, 8 or 16); None: tuned or 1
         self._split = None
         if accumulate not in (None, 'double', 'kahan'):
             raise ValueError(
@@ -786,7 +786,7 @@ class SimulationCUDA(object):
         return 'barrier'
 
     def _split_mode(self):
-        """Warps that share each warp tile's work (1, 2 or 4)."""
+        """Warps that share each warp tile's work (1, 2, 4, 8 or 16)."""
         if self._split is not None:
             return int(self._split)
         if self._block is None:
