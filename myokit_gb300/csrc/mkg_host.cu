@@ -117,23 +117,31 @@ __global__ void k_soa_to_aos(const Real *__restrict__ in, double *out,
  * contiguous run of nvar * MKG_TILE_CELLS doubles, through shared memory,
  * so that the AoS side is read or written in full contiguous runs and the
  * SoA side as MKG_TILE_CELLS consecutive cells per state. Same conversions,
- * bit for bit; no division per element. */
+ * bit for bit. A cell's row sits in shared memory at an odd stride
+ * (nvar | 1 doubles): the 32 cells of one state, read or written by one
+ * warp, then fall in distinct banks (at a stride of nvar doubles, an even
+ * nvar put a half-warp's 16 accesses in one bank). */
 #define MKG_TILE_CELLS 32
 #define MKG_TILE_NVAR 96
+#define MKG_TILE_STRIDE(nvar) ((nvar) | 1)
 
 template <typename Real>
 __global__ void __launch_bounds__(256)
 k_aos_to_soa_tiled(const double *__restrict__ in, Real *out, long long ncell,
                    int nvar, long long pitch, Slots sl, void *alt)
 {
-    __shared__ double tile[MKG_TILE_CELLS * MKG_TILE_NVAR];
+    __shared__ double tile[MKG_TILE_CELLS * MKG_TILE_STRIDE(MKG_TILE_NVAR)];
+    const int stride = MKG_TILE_STRIDE(nvar);
     const long long ntile = (ncell + MKG_TILE_CELLS - 1) / MKG_TILE_CELLS;
     for (long long t = blockIdx.x; t < ntile; t += gridDim.x) {
         const long long c0 = t * MKG_TILE_CELLS;
         const int nc = (int)min((long long)MKG_TILE_CELLS, ncell - c0);
         const int nv = nc * nvar;
         const double *src = in + c0 * nvar;
-        for (int k = threadIdx.x; k < nv; k += blockDim.x) tile[k] = src[k];
+        for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+            const int cc = k / nvar;
+            tile[cc * stride + (k - cc * nvar)] = src[k];
+        }
         __syncthreads();
         for (int k = threadIdx.x; k < nvar * MKG_TILE_CELLS;
              k += blockDim.x) {
@@ -141,7 +149,7 @@ k_aos_to_soa_tiled(const double *__restrict__ in, Real *out, long long ncell,
             const int cc = k - s * MKG_TILE_CELLS;
             if (cc >= nc) continue;
             const long long c = c0 + cc;
-            const double v = tile[cc * nvar + s];
+            const double v = tile[cc * stride + s];
             const int j = sl.hi_slot ? sl.hi_slot[s] : -1;
             if (j >= 0 && sl.hi_mode == MKG_HI_DOUBLE) {
                 if (s == sl.skip_var) ((double *)alt)[c] = v;
@@ -168,7 +176,8 @@ __global__ void __launch_bounds__(256)
 k_soa_to_aos_tiled(const Real *__restrict__ in, double *out, long long ncell,
                    int nvar, long long pitch, Slots sl, const void *alt)
 {
-    __shared__ double tile[MKG_TILE_CELLS * MKG_TILE_NVAR];
+    __shared__ double tile[MKG_TILE_CELLS * MKG_TILE_STRIDE(MKG_TILE_NVAR)];
+    const int stride = MKG_TILE_STRIDE(nvar);
     const long long ntile = (ncell + MKG_TILE_CELLS - 1) / MKG_TILE_CELLS;
     for (long long t = blockIdx.x; t < ntile; t += gridDim.x) {
         const long long c0 = t * MKG_TILE_CELLS;
@@ -190,12 +199,15 @@ k_soa_to_aos_tiled(const Real *__restrict__ in, double *out, long long ncell,
                 v = (double)in[(long long)s * pitch + c];
             if (j >= 0 && sl.hi_mode == MKG_HI_KAHAN)
                 v -= (double)((const Real *)sl.hi)[(long long)j * pitch + c];
-            tile[cc * nvar + s] = v;
+            tile[cc * stride + s] = v;
         }
         __syncthreads();
         const int nv = nc * nvar;
         double *dst = out + c0 * nvar;
-        for (int k = threadIdx.x; k < nv; k += blockDim.x) dst[k] = tile[k];
+        for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+            const int cc = k / nvar;
+            dst[k] = tile[cc * stride + (k - cc * nvar)];
+        }
         __syncthreads();
     }
 }
