@@ -55,6 +55,36 @@ def test_errors_without_handle():
     lib.mkg_destroy(None)   # must be a no-op
 
 
+@pytest.mark.parametrize('split,block,ok', [
+    (3, 128, False), (32, 128, False), (-1, 128, False),
+    (8, 96, False),      # 3 warps: neither whole teams nor whole CTAs
+    (16, 32, False),     # a cluster of 16 CTAs (at most 8)
+    (4, 128, True), (8, 128, True), (16, 128, True), (8, 32, True)])
+def test_create_validates_split(split, block, ok):
+    # Checked before any device call: a refused shape names the rule, an
+    # accepted one fails later for want of a GPU (or a valid kernel image)
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    cfg = _lib.MkgConfig()
+    cfg.nx = 200
+    cfg.ny = 1
+    cfg.real_bytes = 8
+    cfg.n_state = 8
+    cfg.block_x = block
+    cfg.block_y = 1
+    cfg.split = split
+    code = lib.mkg_create(ctypes.byref(cfg), b'x', 1, ctypes.byref(h))
+    assert code != _lib.MKG_OK
+    msg = lib.mkg_last_error(None)
+    if ok:
+        assert b'split' not in msg
+    else:
+        assert code == _lib.MKG_ERR_ARG
+        assert b'split' in msg
+    if h:
+        lib.mkg_destroy(h)
+
+
 def test_compile_error_reports_log():
     with pytest.raises(_lib.MkgError) as e:
         _lib.compile_source('this is not cuda', ['--gpu-architecture=sm_103a'])
