@@ -125,6 +125,22 @@ def _few_tiles(sim):
     return tiles < _sm_count(sim._device)
 
 
+def _candidates(sim):
+    """The launch configurations the tuner times on ``sim``."""
+    double = sim._precision == myokit.DOUBLE_PRECISION
+    # FP64 kernels spill when registers are capped
+    out = list(_CANDIDATES_FP64 if double else _CANDIDATES)
+    if _few_tiles(sim) and sim._accumulate is None:
+        # Cluster teams (more warps per tile than the CTA holds) pay where
+        # a tile's double precision instructions bind; a single precision
+        # small grid is bound by the step's latency, and its cluster
+        # barrier only costs (200-cell cable: 0.074 and 0.065 against
+        # 0.098e9 cell-steps/s)
+        out += [c for c in _CANDIDATES_SPLIT
+                if double or c[5] <= c[0][0] // 32]
+    return out
+
+
 def autotune(sim, duration=None, candidates=None, store=True,
              verbose=False):
     """
@@ -135,11 +151,7 @@ def autotune(sim, duration=None, candidates=None, store=True,
     cell-steps per second of device time.
     """
     if candidates is None:
-        # FP64 kernels spill when registers are capped
-        candidates = _CANDIDATES_FP64 \
-            if sim._precision == myokit.DOUBLE_PRECISION else _CANDIDATES
-        if _few_tiles(sim) and sim._accumulate is None:
-            candidates = list(candidates) + _CANDIDATES_SPLIT
+        candidates = _candidates(sim)
     if duration is None:
         steps = max(20, int(4e8 / sim._ntotal))
         if sim._precision == myokit.DOUBLE_PRECISION:

@@ -112,3 +112,27 @@ def test_shipped_table_and_candidates_are_valid():
             assert bx % 32 == 0 and by == 1 and bx * mb <= 2048
             assert int(lazy) in (0, 1, 2) and spl >= 0
             assert sync in ('barrier', 'neighbors')
+
+
+def test_split_candidates_by_precision(br77):
+    # Small grids try split tiles; cluster teams (8 and 16 warps of
+    # 128-thread CTAs) only in double precision
+    p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+    dp = mg.SimulationCUDA(br77, p, ncells=200,
+                           precision=myokit.DOUBLE_PRECISION)
+    sp = mg.SimulationCUDA(br77, p, ncells=200)
+    kahan = mg.SimulationCUDA(br77, p, ncells=200, accumulate='kahan')
+    big = mg.SimulationCUDA(br77, p, ncells=(512, 512),
+                            precision=myokit.DOUBLE_PRECISION)
+
+    def splits(s):
+        return sorted(c[5] for c in at._candidates(s) if len(c) > 5)
+    assert splits(dp) == [2, 2, 4, 4, 8, 16]
+    assert splits(sp) == [2, 2, 4, 4]
+    assert splits(kahan) == []
+    assert splits(big) == []
+    for c in at._CANDIDATES_SPLIT:
+        (bx, by), mb, spl, lazy, sync, split = c
+        nwarp = bx // 32
+        assert (split <= nwarp and nwarp % split == 0) or (
+            split % nwarp == 0 and split // nwarp <= 8)
