@@ -261,3 +261,56 @@ def test_divided_derivatives_add_up(name, rl):
             1 + sum(abs(c * e.eval(subst=sub)) for c, e in terms))), qname
         checked += 1
     assert checked >= 1
+
+
+def _slot_check(k):
+    """Static checks of a split body's partial-sum hand-over: every slot is
+    written by one warp other than its reader, with a remote store exactly
+    when the two are in different CTAs of the cluster, and read by one
+    owner; indices and ranks are in range."""
+    import re
+    nwarp = k.block[0] // 32
+    parts = re.split(r'\n\s*(?:else )?if \(part_ == (\d+)\) \{', '\n' +
+                     k.split_body)
+    assert [int(p) for p in parts[1::2]] == list(range(k.split))
+    writes, reads = {}, {}
+    for p, body in zip(parts[1::2], parts[2::2]):
+        p = int(p)
+        for slot in re.findall(r'MKG_PP_LOCAL\((\d+),', body):
+            writes.setdefault(int(slot), []).append((p, None))
+        for slot, rank in re.findall(r'MKG_PP_PUT\((\d+), (\d+),', body):
+            writes.setdefault(int(slot), []).append((p, int(rank)))
+        for slot in re.findall(r'MKG_PP_GET\((\d+)\)', body):
+            reads.setdefault(int(slot), []).append(p)
+        # the team barrier comes after every hand-over and before every read
+        sync = body.index('mkg_team_sync();')
+        assert 'MKG_PP_GET' not in body[:sync]
+        assert 'MKG_PP_PUT' not in body[sync:]
+        assert 'MKG_PP_LOCAL' not in body[sync:]
+    assert sorted(writes) == sorted(reads) == list(range(k.split_nslot))
+    for slot in writes:
+        (w, rank), = writes[slot]
+        (r,) = reads[slot]
+        assert w != r
+        if rank is None:
+            assert k.split_cl == 1 or w // nwarp == r // nwarp
+        else:
+            assert k.split_cl > 1 and rank == r // nwarp != w // nwarp
+            assert 0 <= rank < k.split_cl
+
+
+@pytest.mark.parametrize('split,block', [(4, 128), (8, 128), (16, 64)])
+def test_split_hand_over_of_every_model(split, block):
+    # Every model of myokit's test data that the simulation accepts:
+    # the partial-sum slots are consistent and the kernel compiles
+    import test_models as tm
+    for name in tm.ACCEPTED:
+        m = tm._model(name)
+        p = myokit.pacing.blocktrain(period=1000, duration=2, level=1)
+        s = mg.SimulationCUDA(m, p, ncells=100, precision=DP, block=block)
+        s._split = split
+        k = s._kernel([])
+        assert k.split == split, name
+        _slot_check(k)
+        cubin, _ = _lib.compile_source(k.source(), k.options())
+        assert cubin[:4] == b'\x7fELF', name
